@@ -1,0 +1,163 @@
+/*
+ * mepi.h -- C ABI of the GB300 (sm_103a) implementation of MEPinterp's
+ * per-k-point Wannier-interpolation path (AHC + Niu MEP + Kubo MEP).
+ *
+ * The reference has no plugin or FFI layer: its boundary is the body of the
+ * k-loop in src/core.f90:165-270, which calls get_wann_interp
+ * (src/wann_interp.f90:56-108) and the band sums kubo_ahc_tens
+ * (src/kubo.f90:37-78), mep_niu_IC/LC/CS (src/mep_niu.f90:20-159) and
+ * kubo_mep_IC/LC/CS (src/kubo_mep.f90:16-149) once per k-point, adding into
+ * the *_loc accumulators allocated in src/core.f90:610-691.  One mepi_run call
+ * replaces that whole loop for one MPI rank: it returns the same unnormalised
+ * local sums, so fermi_selector and integrate_over_k_space
+ * (src/core.f90:276-292) run unchanged on top of it.
+ *
+ * Conventions
+ *  - All arrays use the reference's Fortran (column-major, 1-based in Fortran)
+ *    layout; complex numbers are interleaved (re, im) doubles.
+ *  - Units are the reference's internal atomic units (Hartree, bohr), i.e.
+ *    what read_tb_basis leaves in memory (src/file_io.f90:741, :790).
+ *  - The caller owns every host buffer; the library owns its device state and
+ *    copies the model to the GPU in mepi_create.
+ *  - Every function returns 0 on success or a MEPI_ERR_* code; nothing exits
+ *    the process (the reference calls `stop`; a Fortran shim maps a nonzero
+ *    status to `stop`).
+ *  - Threading: one context per host thread; calls are synchronous.
+ */
+#ifndef MEPI_H
+#define MEPI_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define MEPI_OK 0
+#define MEPI_ERR_ARG 1          /* bad shape, NULL pointer, bad option */
+#define MEPI_ERR_CUDA 2         /* CUDA runtime error or no usable device */
+#define MEPI_ERR_NOMEM 3        /* device allocation failed */
+#define MEPI_ERR_EIG 4          /* Jacobi eigensolver hit its sweep cap */
+#define MEPI_ERR_NONHERM 5      /* H(R) is not Hermitian: H(-R) != H(R)^dag */
+#define MEPI_ERR_NONFINITE 6    /* NaN/Inf in the input model */
+
+/* semantics where the reference is not reproducible (see mepi_model) */
+#define MEPI_SEM_REF 0
+#define MEPI_SEM_PAPER 1
+
+/* output mask (src/core.f90:198-230: do_mep, do_kubo, do_ahc) */
+#define MEPI_OUT_AHC 1u
+#define MEPI_OUT_MEP_NIU 2u
+#define MEPI_OUT_KUBO_MEP 4u
+
+/* arithmetic form of the run */
+#define MEPI_PREC_FP64 0   /* all-FP64 plain form */
+#define MEPI_PREC_MIXED 1  /* split-FP16 tensor-core Fourier sums, FP32 per-k
+                              work, FP64 k-sums, FP64 rerun of k-points whose
+                              band gap falls below degen_gap */
+
+typedef struct mepi_ctx mepi_ctx;
+
+/* The tight-binding basis: what read_tb_basis (src/file_io.f90:800-860) and
+ * init_parameters (src/input_paras.f90:79-293) leave in memory. */
+typedef struct {
+    int32_t n_wf;              /* number of Wannier functions N */
+    int32_t n_R;               /* number of lattice vectors nR */
+    const double *R_frac;      /* R_frac(3, n_R), lattice units */
+    const double *H;           /* complex H_real(N, N, n_R), Hartree */
+    const double *r;           /* complex r_real(3, N, N, n_R), bohr; NULL = no
+                                  position operator (no A, Omega, CS terms) */
+    const double *wf_centers;  /* wf_centers(3, N), lattice units; NULL selects
+                                  the Wannier phase convention */
+    double a_latt[9];          /* a_latt(3,3) column-major (row i = a_i) */
+    int32_t do_gauge_trafo;    /* [wannInterp] doGaugeTrafo */
+    int32_t use_cart_velo;     /* [wannInterp] use_cart_velo */
+    int32_t semantics;         /* MEPI_SEM_REF: curvature and velocity from
+                                  A^H = A_bar + iD as the reference computes
+                                  them; MEPI_SEM_PAPER: from A_bar */
+    double kubo_tol;           /* [Fermi] kuboTol */
+} mepi_model;
+
+/* One rank's share of the k-loop (src/core.f90:165-270). */
+typedef struct {
+    int32_t mp_grid[3];        /* Monkhorst-Pack mesh */
+    int64_t k_begin;           /* first 0-based linear k index (kx fastest) */
+    int64_t k_stride;          /* stride between owned k; mpi_ki_selector
+                                  (src/mpi_comm.f90:80-99) = rank, nProcs */
+    int64_t k_count;           /* number of k to process; < 0 = all owned */
+    int32_t n_eF;              /* number of Fermi energies */
+    const double *ef_lst;      /* ef_lst(n_eF), Hartree */
+    double T_kelvin;           /* temperature; <= 1e-2 K means a step function */
+    int32_t valence_bands;     /* [MEP] valence_bands (0..N) */
+    uint32_t outputs;          /* MEPI_OUT_* mask */
+    int32_t precision;         /* MEPI_PREC_* */
+    int64_t chunk_k;           /* k-points per device chunk; 0 = automatic */
+    double degen_gap;          /* MEPI_PREC_MIXED only: minimum band gap (Ha)
+                                  for the FP32 per-k path; < 0 = default
+                                  (1e-4 eV) */
+} mepi_job;
+
+/* Unnormalised local sums, like the reference's *_loc arrays
+ * (src/core.f90:610-691).  Each pointer may be NULL when its output is not
+ * requested; buffers are overwritten (not accumulated into). */
+typedef struct {
+    double *Ne_sum;            /* Ne_loc_sum(n_eF) */
+    double *ahc;               /* kubo_ahc_loc(3,3,n_eF) */
+    double *mep_ic;            /* mep_bands_ic_loc(3,3,valence_bands) */
+    double *mep_lc;            /* mep_bands_lc_loc(3,3,valence_bands) */
+    double *mep_cs;            /* mep_bands_cs_loc(3,3,valence_bands) */
+    double *kubo_mep_ic;       /* kubo_mep_ic_loc(3,3,n_eF) */
+    double *kubo_mep_lc;       /* kubo_mep_lc_loc(3,3,n_eF) */
+    double *kubo_mep_cs;       /* kubo_mep_cs_loc(3,3,n_eF) */
+    int64_t n_k_done;          /* n_ki_loc */
+    int64_t n_k_fp64;          /* MEPI_PREC_MIXED: k-points rerun in FP64 */
+    int32_t eig_max_sweeps;    /* largest Jacobi sweep count seen */
+} mepi_acc;
+
+/* Device time of each stage of the last mepi_run (CUDA events on the
+ * library's stream), milliseconds, with launch counts. */
+typedef struct {
+    double ft_ms;              /* Fourier sums (SIMT FP64 or tensor-core GEMM) */
+    double phase_ms;           /* mixed form: phase-operand generation */
+    double eig_ms, rot_ms, gauge_ms, bandsum_ms, reduce_ms;
+    double total_ms;           /* sum of the stage times */
+    double run_ms;             /* whole call, first launch to last copy back */
+    int32_t ft_launches, phase_launches, eig_launches, rot_launches, gauge_launches, bandsum_launches,
+        reduce_launches;
+    int64_t n_k;               /* k-points of the run */
+    int64_t h2d_bytes;         /* host->device bytes since mepi_create */
+    int64_t d2h_bytes;         /* device->host bytes since mepi_create */
+} mepi_timing;
+
+/* Replaces read_tb_basis's arrays being handed to get_wann_interp
+ * (src/core.f90:144, :179-182): validates and uploads the model. */
+int mepi_create(mepi_ctx **out, const mepi_model *m);
+
+/* Replaces the k-loop body src/core.f90:165-270 for one rank. */
+int mepi_run(mepi_ctx *ctx, const mepi_job *job, mepi_acc *out);
+
+/* Per-k results of get_wann_interp (src/wann_interp.f90:56-108) for a list of
+ * k-points given in lattice units (kpts(3, n_k)): eigenvalues en_k(N, n_k),
+ * velocities V_ka(3, N, N, n_k) complex; A_diag(3, N, n_k) and
+ * Om_diag(3, 3, N, n_k) complex hold the band-diagonal connection and
+ * curvature (the parts the band sums consume); either may be NULL. */
+int mepi_interp_k(mepi_ctx *ctx, int32_t precision, int64_t n_k, const double *kpts,
+                  double *en_k, double *V_ka, double *A_diag, double *Om_diag);
+
+/* Device time per stage of the last mepi_run. */
+int mepi_get_timing(const mepi_ctx *ctx, mepi_timing *t);
+
+/* Frees the context and its device memory. */
+int mepi_destroy(mepi_ctx *ctx);
+
+/* Static message for a status code. */
+const char *mepi_strerror(int status);
+
+/* Library version string. */
+const char *mepi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MEPI_H */

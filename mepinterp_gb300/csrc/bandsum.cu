@@ -1,0 +1,297 @@
+// Band sums of one rank's k-points, accumulated over k in FP64:
+//   kubo_ahc_tens (src/kubo.f90:37-78)
+//       curv(i,j,n) = -2 sum_{m!=n} Im(V_i(n,m) V_j(m,n)) / (E_m - E_n)^2
+//       ahc(i,j,e) -= sum_n curv(i,j,n) f(e,n)
+//   mep_niu_IC / kubo_mep_IC (src/mep_niu.f90:102-159, src/kubo_mep.f90:100-149)
+//       F2(i,j,n0) = -sum_{n,m != n0} Re(V_i(n0,n) (V(n,m) x V(m,n0))_j)
+//                                     / ((E0-En)^2 (E0-Em))
+//   mep_niu_LC / kubo_mep_LC (src/mep_niu.f90:47-99, src/kubo_mep.f90:51-97)
+//       F3(i,j,n0) = sum_{n != n0} Re(V_i(n0,n) (V(n,n0) x V(n0,n0))_j) / (E0-En)^3
+//   mep_niu_CS / kubo_mep_CS: per-band value csv(n0) from the gauge kernel.
+// (x is the Levi-Civita contraction sum_kl eps_jkl a_k b_l.)  The Niu sums run
+// over n0 < valence_bands and skip terms whose product denominator satisfies
+// |den| <= kuboTol, exactly as the reference; the Kubo sums run over all n0,
+// weight by f(e,n0) and have no guard (D9).
+//
+// Work split: the CTA stages V (row stride N+1) in shared memory; warp w
+// handles bands n0 = w, w + nwarps, ...; lane l handles n = l, l+32 and loops
+// over m for the IC contraction, then the warp reduces the per-band tensors.
+// The Fermi contraction runs one thread (nE >= 64) or one warp (nE < 64) per
+// Fermi energy.  A CTA owns one FP64 accumulator slice for its whole k stripe
+// (k = blockIdx.x, blockIdx.x + gridDim.x, ...), so the final reduction over
+// slices runs in a fixed order and the result is deterministic.
+#include "mepi_internal.cuh"
+
+namespace mepi {
+
+namespace {
+
+template <typename T>
+__device__ __forceinline__ T fd_stat(T e_band, double e_fermi, double T_kelvin) {  // src/statistics.f90:65-90
+    if (T_kelvin > kMinTemp) {
+        double x = ((double)e_band - e_fermi) / (kKbEhK * T_kelvin);
+        return (T)(1.0 / (1.0 + exp(x)));
+    }
+    return ((double)e_band < e_fermi) ? (T)1 : (T)0;
+}
+
+// cross(a, b)_j = sum_kl eps_jkl a_k b_l
+template <typename T>
+__device__ __forceinline__ void cross3(const cplx<T> a[3], const cplx<T> b[3], cplx<T> out[3]) {
+    out[0] = a[1] * b[2] - a[2] * b[1];
+    out[1] = a[2] * b[0] - a[0] * b[2];
+    out[2] = a[0] * b[1] - a[1] * b[0];
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) bandsum_kernel(DevModel md, JobDev jb, int64_t nk, const T* __restrict__ Eg,
+                                                      const cplx<T>* __restrict__ Vg, const T* __restrict__ CSVg,
+                                                      const int* __restrict__ skip, double* __restrict__ partials) {
+    extern __shared__ unsigned char smem_raw[];
+    const int N = md.N, NN = N * N, ld = N + 1;
+    const int nval = jb.nval, nE = jb.nE;
+    cplx<T>* Vs = reinterpret_cast<cplx<T>*>(smem_raw);          // [3][N][ld]
+    double* curv = reinterpret_cast<double*>(Vs + 3 * N * ld);    // [9][N]
+    double* icn = curv + 9 * N;                                   // [9][N] Kubo IC per band
+    double* lcn = icn + 9 * N;                                    // [9][N] Kubo LC per band
+    double* icv = lcn + 9 * N;                                    // [9][kMaxN] Niu IC
+    double* lcv = icv + 9 * kMaxN;                                // [9][kMaxN] Niu LC
+    T* Es = reinterpret_cast<T*>(lcv + 9 * kMaxN);                // [N]
+    T* Cs = Es + kMaxN;                                           // [N]
+    const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nwarps = nt >> 5;
+    const AccLayout L{nE, nval};
+    double* P = partials + (size_t)blockIdx.x * L.size();
+    const double tol = md.kubo_tol;
+
+    for (int64_t k = blockIdx.x; k < nk; k += gridDim.x) {
+        if (skip && skip[k]) continue;
+        __syncthreads();
+        for (int e = tid; e < 3 * NN; e += nt) {
+            int a = e / NN, r = e % NN, n = r / N, m = r % N;
+            Vs[(a * N + n) * ld + m] = Vg[(size_t)k * 3 * NN + e];
+        }
+        for (int n = tid; n < N; n += nt) {
+            Es[n] = Eg[(size_t)k * N + n];
+            Cs[n] = CSVg ? CSVg[(size_t)k * N + n] : (T)0;
+        }
+        __syncthreads();
+        auto V = [&](int a, int n, int m) -> cplx<T> { return Vs[(a * N + n) * ld + m]; };
+
+        for (int n0 = warp; n0 < N; n0 += nwarps) {
+            const T E0 = Es[n0];
+            const bool niu = (n0 < nval) && jb.do_mep;
+            double s_curv[9], s_ic[9], s_lc[9], s_icv[9], s_lcv[9];
+#pragma unroll
+            for (int q = 0; q < 9; ++q) s_curv[q] = s_ic[q] = s_lc[q] = s_icv[q] = s_lcv[q] = 0.0;
+            cplx<T> vnn[3];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) vnn[c] = V(c, n0, n0);
+            for (int n = lane; n < N; n += 32) {
+                if (n == n0) continue;
+                const T En = Es[n];
+                const T d0n = E0 - En;  // E0 - En
+                cplx<T> vi[3], vk[3];
+#pragma unroll
+                for (int c = 0; c < 3; ++c) { vi[c] = V(c, n0, n); vk[c] = V(c, n, n0); }
+                // AHC: curv(i,j,n0) = -2 Im(V_i(n0,n) V_j(n,n0)) / (En - E0)^2
+                if (jb.do_ahc) {
+                    T inv = (T)1 / (d0n * d0n);
+#pragma unroll
+                    for (int j = 0; j < 3; ++j)
+#pragma unroll
+                        for (int i = 0; i < 3; ++i) s_curv[i + 3 * j] += -2.0 * (double)((vi[i] * vk[j]).im * inv);
+                }
+                // LC
+                {
+                    cplx<T> x[3];
+                    cross3(vk, vnn, x);
+                    T den3 = d0n * d0n * d0n;
+                    bool kubo_ok = jb.do_kubo;
+                    bool niu_ok = niu && (fabs((double)den3) > tol);
+                    if (kubo_ok || niu_ok) {
+#pragma unroll
+                        for (int j = 0; j < 3; ++j)
+#pragma unroll
+                            for (int i = 0; i < 3; ++i) {
+                                double v = (double)((vi[i] * x[j]).re / den3);
+                                if (kubo_ok) s_lc[i + 3 * j] += v;
+                                if (niu_ok) s_lcv[i + 3 * j] += v;
+                            }
+                    }
+                }
+                // IC: g_j = sum_{m != n0} (V(n,m) x V(m,n0))_j / (E0 - Em)
+                if (jb.do_kubo || niu) {
+                    cplx<T> g[3], gv[3];
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) g[c] = gv[c] = mk((T)0, (T)0);
+                    const T a2 = d0n * d0n;
+                    for (int m = 0; m < N; ++m) {
+                        if (m == n0) continue;
+                        cplx<T> vnm[3], vmo[3], x[3];
+#pragma unroll
+                        for (int c = 0; c < 3; ++c) { vnm[c] = V(c, n, m); vmo[c] = V(c, m, n0); }
+                        cross3(vnm, vmo, x);
+                        const T d0m = E0 - Es[m];
+                        const T b = (T)1 / d0m;
+#pragma unroll
+                        for (int c = 0; c < 3; ++c) g[c] = g[c] + b * x[c];
+                        if (niu && fabs((double)(a2 * d0m)) > tol) {
+#pragma unroll
+                            for (int c = 0; c < 3; ++c) gv[c] = gv[c] + b * x[c];
+                        }
+                    }
+                    const T ainv = (T)1 / a2;
+#pragma unroll
+                    for (int j = 0; j < 3; ++j)
+#pragma unroll
+                        for (int i = 0; i < 3; ++i) {
+                            s_ic[i + 3 * j] += -(double)((vi[i] * g[j]).re * ainv);
+                            s_icv[i + 3 * j] += -(double)((vi[i] * gv[j]).re * ainv);
+                        }
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < 9; ++q) {
+                double a = warp_sum(s_curv[q]), b = warp_sum(s_ic[q]), c = warp_sum(s_lc[q]);
+                double d = warp_sum(s_icv[q]), e = warp_sum(s_lcv[q]);
+                if (lane == 0) {
+                    curv[q * N + n0] = a;
+                    icn[q * N + n0] = b;
+                    lcn[q * N + n0] = c;
+                    if (n0 < kMaxN) { icv[q * kMaxN + n0] = d; lcv[q * kMaxN + n0] = e; }
+                }
+            }
+        }
+        __syncthreads();
+        // Niu MEP: band resolved, no occupation weight
+        if (jb.do_mep) {
+            for (int t = tid; t < 9 * nval; t += nt) {
+                int q = t % 9, n0 = t / 9;
+                P[L.mic_off() + q + 9 * n0] += icv[q * kMaxN + n0];
+                P[L.mlc_off() + q + 9 * n0] += lcv[q * kMaxN + n0];
+                if (q == 0 || q == 4 || q == 8) P[L.mcs_off() + q + 9 * n0] += (double)Cs[n0];
+            }
+        }
+        // Fermi contraction
+        if (nE >= 64) {
+            for (int e = tid; e < nE; e += nt) {
+                const double ef = jb.ef[e];
+                double ne = 0, a[9], ki[9], kl[9], kc = 0;
+#pragma unroll
+                for (int q = 0; q < 9; ++q) a[q] = ki[q] = kl[q] = 0;
+                for (int n = 0; n < N; ++n) {
+                    double f = (double)fd_stat<T>(Es[n], ef, jb.T_kelvin);
+                    ne += f;
+                    kc += f * (double)Cs[n];
+#pragma unroll
+                    for (int q = 0; q < 9; ++q) {
+                        a[q] -= curv[q * N + n] * f;
+                        ki[q] += icn[q * N + n] * f;
+                        kl[q] += lcn[q * N + n] * f;
+                    }
+                }
+                P[L.ne_off() + e] += ne;
+                if (jb.do_ahc)
+                    for (int q = 0; q < 9; ++q) P[L.ahc_off() + q + 9 * e] += a[q];
+                if (jb.do_kubo) {
+                    for (int q = 0; q < 9; ++q) {
+                        P[L.kic_off() + q + 9 * e] += ki[q];
+                        P[L.klc_off() + q + 9 * e] += kl[q];
+                    }
+                    P[L.kcs_off() + 0 + 9 * e] += kc;
+                    P[L.kcs_off() + 4 + 9 * e] += kc;
+                    P[L.kcs_off() + 8 + 9 * e] += kc;
+                }
+            }
+        } else {
+            for (int e = warp; e < nE; e += nwarps) {
+                const double ef = jb.ef[e];
+                double ne = 0, a[9], ki[9], kl[9], kc = 0;
+#pragma unroll
+                for (int q = 0; q < 9; ++q) a[q] = ki[q] = kl[q] = 0;
+                for (int n = lane; n < N; n += 32) {
+                    double f = (double)fd_stat<T>(Es[n], ef, jb.T_kelvin);
+                    ne += f;
+                    kc += f * (double)Cs[n];
+#pragma unroll
+                    for (int q = 0; q < 9; ++q) {
+                        a[q] -= curv[q * N + n] * f;
+                        ki[q] += icn[q * N + n] * f;
+                        kl[q] += lcn[q * N + n] * f;
+                    }
+                }
+                ne = warp_sum(ne);
+                kc = warp_sum(kc);
+#pragma unroll
+                for (int q = 0; q < 9; ++q) { a[q] = warp_sum(a[q]); ki[q] = warp_sum(ki[q]); kl[q] = warp_sum(kl[q]); }
+                if (lane == 0) {
+                    P[L.ne_off() + e] += ne;
+                    if (jb.do_ahc)
+                        for (int q = 0; q < 9; ++q) P[L.ahc_off() + q + 9 * e] += a[q];
+                    if (jb.do_kubo) {
+                        for (int q = 0; q < 9; ++q) {
+                            P[L.kic_off() + q + 9 * e] += ki[q];
+                            P[L.klc_off() + q + 9 * e] += kl[q];
+                        }
+                        P[L.kcs_off() + 0 + 9 * e] += kc;
+                        P[L.kcs_off() + 4 + 9 * e] += kc;
+                        P[L.kcs_off() + 8 + 9 * e] += kc;
+                    }
+                }
+            }
+        }
+    }
+}
+
+__global__ void reduce_kernel(const double* __restrict__ partials, int n_cta, int size, double* __restrict__ out) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < size; i += gridDim.x * blockDim.x) {
+        double s = 0.0;
+        for (int c = 0; c < n_cta; ++c) s += partials[(size_t)c * size + i];
+        out[i] = s;
+    }
+}
+
+}  // namespace
+
+int bandsum_ctas() {
+    int dev = 0, sms = 148;
+    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return 2 * sms;
+}
+
+template <typename T>
+size_t bandsum_smem(int N) {
+    size_t b = 3 * (size_t)N * (N + 1) * sizeof(cplx<T>);
+    b += (27 * (size_t)N + 18 * kMaxN) * sizeof(double);
+    b += 2 * kMaxN * sizeof(T);
+    return (b + 15) & ~(size_t)15;
+}
+
+template <typename T>
+cudaError_t launch_bandsum(const DevModel& m, const JobDev& j, int64_t nk, const T* E, const cplx<T>* V, const T* CSV,
+                           const int* skip, double* partials, int n_cta, cudaStream_t s) {
+    if (nk <= 0) return cudaSuccess;
+    size_t smem = bandsum_smem<T>(m.N);
+    cudaError_t e = cudaFuncSetAttribute(bandsum_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    bandsum_kernel<T><<<n_cta, 256, smem, s>>>(m, j, nk, E, V, CSV, skip, partials);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_reduce(const double* partials, int n_cta, int size, double* out, cudaStream_t s) {
+    reduce_kernel<<<(size + 255) / 256, 256, 0, s>>>(partials, n_cta, size, out);
+    return cudaGetLastError();
+}
+
+template cudaError_t launch_bandsum<double>(const DevModel&, const JobDev&, int64_t, const double*,
+                                            const cplx<double>*, const double*, const int*, double*, int, cudaStream_t);
+template cudaError_t launch_bandsum<float>(const DevModel&, const JobDev&, int64_t, const float*, const cplx<float>*,
+                                           const float*, const int*, double*, int, cudaStream_t);
+
+}  // namespace mepi

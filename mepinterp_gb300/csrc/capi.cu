@@ -1,0 +1,623 @@
+// C ABI of libmepi_gb300 (declared in include/mepi.h).
+//
+// mepi_create  validates the tight-binding basis (shapes, finiteness,
+//              H(-R) = H(R)^dag) and uploads the Fourier stack S[R][pair][blk]
+//              (see mepi_internal.cuh) built on the host in FP64.
+// mepi_run     replaces the k-loop of src/core.f90:165-270 for one rank: the
+//              owned k-points are streamed through the device in chunks
+//              (FT -> eigensolve -> rotation -> gauge/velocity -> band sums),
+//              the band sums accumulate into per-CTA FP64 slices that persist
+//              across chunks, and one fixed-order reduction produces the
+//              reference's *_loc sums.  In the mixed form the chunk runs in
+//              FP32 and every k-point whose Jacobi did not converge or whose
+//              smallest band gap is below degen_gap is skipped there and rerun
+//              through the FP64 pipeline afterwards.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "../../include/mepi.h"
+#include "ft_tc.cuh"
+#include "mepi_internal.cuh"
+
+using namespace mepi;
+
+namespace {
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    cudaError_t ensure(size_t b) {
+        if (b <= bytes) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+        cudaError_t e = cudaMalloc(&p, b);
+        if (e == cudaSuccess) bytes = b;
+        return e;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    template <typename X> X* as() const { return reinterpret_cast<X*>(p); }
+};
+
+struct StageEv {
+    cudaEvent_t a, b;
+    int stage;
+};
+
+enum { ST_FT = 0, ST_PHASE, ST_EIG, ST_ROT, ST_GAUGE, ST_BAND, ST_RED, ST_RUN, ST_N };
+
+}  // namespace
+
+struct mepi_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    DevModel dm{};
+    int N = 0, nR = 0, nb = 0;
+    double a_latt[9];
+    DevBuf S, R, tau;
+    // per-chunk work buffers
+    DevBuf W, E, U, HA, OD, V, CSV, ODH, flags, klist, kpts, partials, out, counters;
+    int* h_flags = nullptr;  // pinned
+    size_t h_flags_cap = 0;
+    std::vector<StageEv> events;
+    size_t ev_used = 0;
+    mepi_timing timing{};
+    int64_t h2d = 0, d2h = 0;           // host<->device byte counters
+    std::vector<cplx<double>> S_host;  // FP64 stack, kept to build the tensor-core operands
+    TcPlan tc;
+    bool ft_simt_only = false;          // MEPI_FT_SIMT=1: FP64 SIMT Fourier sums in the mixed form too
+};
+
+namespace {
+
+#define CK(x)                                         \
+    do {                                              \
+        cudaError_t _e = (x);                         \
+        if (_e != cudaSuccess) return MEPI_ERR_CUDA;  \
+    } while (0)
+
+#define CKM(x)                                                                       \
+    do {                                                                             \
+        cudaError_t _e = (x);                                                        \
+        if (_e == cudaErrorMemoryAllocation) { cudaGetLastError(); return MEPI_ERR_NOMEM; } \
+        if (_e != cudaSuccess) return MEPI_ERR_CUDA;                                 \
+    } while (0)
+
+int stage_begin(mepi_ctx* c, int stage, size_t* idx) {
+    if (c->ev_used == c->events.size()) {
+        StageEv ev{};
+        CK(cudaEventCreate(&ev.a));
+        CK(cudaEventCreate(&ev.b));
+        c->events.push_back(ev);
+    }
+    *idx = c->ev_used++;
+    c->events[*idx].stage = stage;
+    CK(cudaEventRecord(c->events[*idx].a, c->stream));
+    return 0;
+}
+int stage_end(mepi_ctx* c, size_t idx) {
+    CK(cudaEventRecord(c->events[idx].b, c->stream));
+    return 0;
+}
+
+#define STAGE(st, call)                                   \
+    do {                                                  \
+        size_t _i;                                        \
+        int _r = stage_begin(ctx, st, &_i);               \
+        if (_r) return _r;                                \
+        CK(call);                                         \
+        _r = stage_end(ctx, _i);                          \
+        if (_r) return _r;                                \
+    } while (0)
+
+bool finite_all(const double* p, size_t n) {
+    for (size_t i = 0; i < n; ++i)
+        if (!std::isfinite(p[i])) return false;
+    return true;
+}
+
+template <typename T>
+size_t per_k_bytes(int N, int nb) {
+    size_t NN = (size_t)N * N;
+    return sizeof(cplx<T>) * (nb * NN + NN + 6 * NN + 3 * N + 3 * NN + 3 * N) + sizeof(T) * 2 * N + sizeof(int) +
+           sizeof(int64_t);
+}
+
+template <typename T>
+int ensure_chunk(mepi_ctx* ctx, int64_t chunk) {
+    const size_t NN = (size_t)ctx->N * ctx->N, N = ctx->N;
+    CKM(ctx->W.ensure(chunk * ctx->nb * NN * sizeof(cplx<T>)));
+    CKM(ctx->E.ensure(chunk * N * sizeof(T)));
+    CKM(ctx->U.ensure(chunk * NN * sizeof(cplx<T>)));
+    CKM(ctx->HA.ensure(chunk * 6 * NN * sizeof(cplx<T>)));
+    CKM(ctx->OD.ensure(chunk * 3 * N * sizeof(cplx<T>)));
+    CKM(ctx->V.ensure(chunk * 3 * NN * sizeof(cplx<T>)));
+    CKM(ctx->CSV.ensure(chunk * N * sizeof(T)));
+    CKM(ctx->flags.ensure(chunk * sizeof(int)));
+    return 0;
+}
+
+// One chunk of k-points through FT -> eig -> rot -> gauge (-> bandsum).
+template <typename T>
+int run_chunk(mepi_ctx* ctx, const KRange& kr, const JobDev* jb, int n_cta, double degen_gap, bool want_flags,
+              bool bandsum, cplx<T>* odh) {
+    const int64_t nk = kr.count;
+    int* counters = ctx->counters.as<int>();
+    if (sizeof(T) == 4 && !ctx->ft_simt_only) {
+        if (!ctx->tc.ready()) {
+            int rc = tc_plan_init(ctx->tc, ctx->dm, ctx->S_host.data());
+            if (rc) return rc;
+            ctx->h2d += 2 * (int64_t)ctx->tc.ncolp * ctx->tc.Kp * sizeof(__half);
+        }
+        int rc = tc_plan_rows(ctx->tc, nk);
+        if (rc) return rc;
+        STAGE(ST_PHASE, launch_phase_split(ctx->tc, kr, ctx->stream));
+        STAGE(ST_FT, launch_ft_tc(ctx->tc, kr, reinterpret_cast<cplx<float>*>(ctx->W.p), ctx->stream));
+    } else {
+        STAGE(ST_FT, (launch_ft_simt<T>(ctx->dm, kr, ctx->W.as<cplx<T>>(), ctx->stream)));
+    }
+    STAGE(ST_EIG, (launch_eig<T>(ctx->N, nk, ctx->W.as<cplx<T>>(), ctx->nb, ctx->E.as<T>(), ctx->U.as<cplx<T>>(), 40,
+                                 counters, counters + (sizeof(T) == 8 ? 1 : 2), degen_gap, want_flags ? ctx->flags.as<int>() : nullptr,
+                                 ctx->stream)));
+    STAGE(ST_ROT, (launch_rot<T>(ctx->dm, nk, ctx->W.as<cplx<T>>(), ctx->U.as<cplx<T>>(), ctx->HA.as<cplx<T>>(),
+                                 ctx->OD.as<cplx<T>>(), ctx->stream)));
+    STAGE(ST_GAUGE, (launch_gauge<T>(ctx->dm, nk, ctx->E.as<T>(), ctx->HA.as<cplx<T>>(), ctx->OD.as<cplx<T>>(),
+                                     ctx->V.as<cplx<T>>(), ctx->CSV.as<T>(), odh, ctx->stream)));
+    if (bandsum)
+        STAGE(ST_BAND, (launch_bandsum<T>(ctx->dm, *jb, nk, ctx->E.as<T>(), ctx->V.as<cplx<T>>(), ctx->CSV.as<T>(),
+                                          want_flags ? ctx->flags.as<int>() : nullptr, ctx->partials.as<double>(),
+                                          n_cta, ctx->stream)));
+    return 0;
+}
+
+int collect_timing(mepi_ctx* ctx, int64_t nk) {
+    mepi_timing t{};
+    t.n_k = nk;
+    for (size_t i = 0; i < ctx->ev_used; ++i) {
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, ctx->events[i].a, ctx->events[i].b));
+        switch (ctx->events[i].stage) {
+            case ST_FT: t.ft_ms += ms; t.ft_launches++; break;
+            case ST_PHASE: t.phase_ms += ms; t.phase_launches++; break;
+            case ST_EIG: t.eig_ms += ms; t.eig_launches++; break;
+            case ST_ROT: t.rot_ms += ms; t.rot_launches++; break;
+            case ST_GAUGE: t.gauge_ms += ms; t.gauge_launches++; break;
+            case ST_BAND: t.bandsum_ms += ms; t.bandsum_launches++; break;
+            case ST_RED: t.reduce_ms += ms; t.reduce_launches++; break;
+            case ST_RUN: t.run_ms += ms; break;
+            default: break;
+        }
+    }
+    t.total_ms = t.ft_ms + t.phase_ms + t.eig_ms + t.rot_ms + t.gauge_ms + t.bandsum_ms + t.reduce_ms;
+    t.h2d_bytes = ctx->h2d;
+    t.d2h_bytes = ctx->d2h;
+    ctx->timing = t;
+    return 0;
+}
+
+int64_t default_chunk(int N, int nb, bool fp64) {
+    size_t per = fp64 ? per_k_bytes<double>(N, nb) : per_k_bytes<float>(N, nb);
+    size_t budget = fp64 ? ((size_t)3 << 30) : ((size_t)8 << 30);
+    int64_t c = (int64_t)(budget / per);
+    c = std::min<int64_t>(c, fp64 ? 16384 : 65536);
+    c = std::max<int64_t>(64, c & ~(int64_t)63);
+    return c;
+}
+
+int run_impl(mepi_ctx* ctx, const mepi_job* job, mepi_acc* out) {
+    const int N = ctx->N;
+    const int64_t nk_tot = (int64_t)job->mp_grid[0] * job->mp_grid[1] * job->mp_grid[2];
+    if (job->mp_grid[0] <= 0 || job->mp_grid[1] <= 0 || job->mp_grid[2] <= 0) return MEPI_ERR_ARG;
+    if (job->k_stride <= 0 || job->k_begin < 0) return MEPI_ERR_ARG;
+    if (job->n_eF <= 0 || !job->ef_lst || job->valence_bands < 0 || job->valence_bands > N) return MEPI_ERR_ARG;
+    if (job->precision != MEPI_PREC_FP64 && job->precision != MEPI_PREC_MIXED) return MEPI_ERR_ARG;
+    if (!finite_all(job->ef_lst, job->n_eF) || !std::isfinite(job->T_kelvin)) return MEPI_ERR_ARG;
+    int64_t owned = job->k_begin < nk_tot ? (nk_tot - job->k_begin + job->k_stride - 1) / job->k_stride : 0;
+    int64_t count = job->k_count < 0 ? owned : std::min<int64_t>(job->k_count, owned);
+    const bool fp64 = job->precision == MEPI_PREC_FP64;
+    int64_t chunk = job->chunk_k > 0 ? job->chunk_k : default_chunk(N, ctx->nb, fp64);
+    chunk = std::max<int64_t>(1, std::min<int64_t>(chunk, std::max<int64_t>(count, 1)));
+    const double degen_gap = job->degen_gap >= 0 ? job->degen_gap : 1e-4 / kAuToEv;
+
+    AccLayout L{job->n_eF, job->valence_bands};
+    const int n_cta = bandsum_ctas();
+    CKM(ctx->partials.ensure((size_t)n_cta * L.size() * sizeof(double)));
+    CKM(ctx->out.ensure((size_t)L.size() * sizeof(double) + (size_t)job->n_eF * sizeof(double)));
+    CKM(ctx->counters.ensure(4 * sizeof(int)));
+    CK(cudaMemsetAsync(ctx->partials.p, 0, (size_t)n_cta * L.size() * sizeof(double), ctx->stream));
+    CK(cudaMemsetAsync(ctx->counters.p, 0, 4 * sizeof(int), ctx->stream));
+    ctx->ev_used = 0;
+    size_t run_ev;
+    if (int r0 = stage_begin(ctx, ST_RUN, &run_ev)) return r0;
+    double* d_ef = ctx->out.as<double>() + L.size();
+    CK(cudaMemcpyAsync(d_ef, job->ef_lst, job->n_eF * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    ctx->h2d += job->n_eF * sizeof(double);
+    JobDev jb;
+    jb.nE = job->n_eF;
+    jb.nval = job->valence_bands;
+    jb.do_ahc = (job->outputs & MEPI_OUT_AHC) ? 1 : 0;
+    jb.do_mep = (job->outputs & MEPI_OUT_MEP_NIU) ? 1 : 0;
+    jb.do_kubo = (job->outputs & MEPI_OUT_KUBO_MEP) ? 1 : 0;
+    jb.T_kelvin = job->T_kelvin;
+    jb.ef = d_ef;
+
+    std::vector<int64_t> redo;
+    int rc = 0;
+    if (fp64) {
+        rc = ensure_chunk<double>(ctx, chunk);
+        if (rc) return rc;
+        for (int64_t c0 = 0; c0 < count; c0 += chunk) {
+            KRange kr{job->k_begin + c0 * job->k_stride, job->k_stride, std::min(chunk, count - c0), nullptr, nullptr,
+                      {job->mp_grid[0], job->mp_grid[1], job->mp_grid[2]}};
+            rc = run_chunk<double>(ctx, kr, &jb, n_cta, 0.0, false, true, nullptr);
+            if (rc) return rc;
+        }
+    } else {
+        rc = ensure_chunk<float>(ctx, chunk);
+        if (rc) return rc;
+        const int64_t nchunks = (count + chunk - 1) / chunk;
+        if ((size_t)count > ctx->h_flags_cap) {
+            if (ctx->h_flags) cudaFreeHost(ctx->h_flags);
+            ctx->h_flags = nullptr;
+            ctx->h_flags_cap = 0;
+            CKM(cudaMallocHost(&ctx->h_flags, std::max<int64_t>(count, 1) * sizeof(int)));
+            ctx->h_flags_cap = count;
+        }
+        for (int64_t ci = 0; ci < nchunks; ++ci) {
+            int64_t c0 = ci * chunk, cn = std::min(chunk, count - c0);
+            KRange kr{job->k_begin + c0 * job->k_stride, job->k_stride, cn, nullptr, nullptr,
+                      {job->mp_grid[0], job->mp_grid[1], job->mp_grid[2]}};
+            rc = run_chunk<float>(ctx, kr, &jb, n_cta, degen_gap, true, true, nullptr);
+            if (rc) return rc;
+            CK(cudaMemcpyAsync(ctx->h_flags + c0, ctx->flags.p, cn * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+            ctx->d2h += cn * sizeof(int);
+        }
+        CK(cudaStreamSynchronize(ctx->stream));
+        for (int64_t i = 0; i < count; ++i)
+            if (ctx->h_flags[i]) redo.push_back(job->k_begin + i * job->k_stride);
+        if (!redo.empty()) {
+            int64_t rchunk = std::min<int64_t>(default_chunk(N, ctx->nb, true), (int64_t)redo.size());
+            rc = ensure_chunk<double>(ctx, rchunk);
+            if (rc) return rc;
+            CKM(ctx->klist.ensure(redo.size() * sizeof(int64_t)));
+            CK(cudaMemcpyAsync(ctx->klist.p, redo.data(), redo.size() * sizeof(int64_t), cudaMemcpyHostToDevice,
+                               ctx->stream));
+            ctx->h2d += redo.size() * sizeof(int64_t);
+            for (int64_t c0 = 0; c0 < (int64_t)redo.size(); c0 += rchunk) {
+                KRange kr{0, 1, std::min<int64_t>(rchunk, (int64_t)redo.size() - c0), ctx->klist.as<int64_t>() + c0,
+                          nullptr, {job->mp_grid[0], job->mp_grid[1], job->mp_grid[2]}};
+                rc = run_chunk<double>(ctx, kr, &jb, n_cta, 0.0, false, true, nullptr);
+                if (rc) return rc;
+            }
+        }
+    }
+    STAGE(ST_RED, launch_reduce(ctx->partials.as<double>(), n_cta, L.size(), ctx->out.as<double>(), ctx->stream));
+    std::vector<double> h(L.size());
+    int hc[4] = {0, 0, 0, 0};
+    CK(cudaMemcpyAsync(h.data(), ctx->out.p, L.size() * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpyAsync(hc, ctx->counters.p, 4 * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    ctx->d2h += L.size() * sizeof(double) + 4 * sizeof(int);
+    if (int r1 = stage_end(ctx, run_ev)) return r1;
+    CK(cudaStreamSynchronize(ctx->stream));
+    CK(cudaGetLastError());
+    if (ctx->tc.err) {
+        int terr = 0;
+        CK(cudaMemcpy(&terr, ctx->tc.err, sizeof(int), cudaMemcpyDeviceToHost));
+        if (terr) return MEPI_ERR_CUDA;
+    }
+    rc = collect_timing(ctx, count);
+    if (rc) return rc;
+    const int nE = job->n_eF, nv = job->valence_bands;
+    auto put = [&](double* dst, int off, int n) {
+        if (dst) std::memcpy(dst, h.data() + off, n * sizeof(double));
+    };
+    put(out->Ne_sum, L.ne_off(), nE);
+    put(out->ahc, L.ahc_off(), 9 * nE);
+    put(out->kubo_mep_ic, L.kic_off(), 9 * nE);
+    put(out->kubo_mep_lc, L.klc_off(), 9 * nE);
+    put(out->kubo_mep_cs, L.kcs_off(), 9 * nE);
+    put(out->mep_ic, L.mic_off(), 9 * nv);
+    put(out->mep_lc, L.mlc_off(), 9 * nv);
+    put(out->mep_cs, L.mcs_off(), 9 * nv);
+    out->n_k_done = count;
+    out->n_k_fp64 = fp64 ? count : (int64_t)redo.size();
+    out->eig_max_sweeps = hc[0];
+    // counters[1] counts FP64 Jacobi launches that hit the sweep cap (an error);
+    // FP32 cap hits (counters[2]) were flagged and rerun in FP64.
+    if (hc[1] > 0) return MEPI_ERR_EIG;
+    return MEPI_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* mepi_version(void) { return "mepinterp-gb300 0.1 (sm_103a)"; }
+
+const char* mepi_strerror(int s) {
+    switch (s) {
+        case MEPI_OK: return "ok";
+        case MEPI_ERR_ARG: return "invalid argument (shape, pointer or option)";
+        case MEPI_ERR_CUDA: return "CUDA error or no usable GPU";
+        case MEPI_ERR_NOMEM: return "device memory allocation failed";
+        case MEPI_ERR_EIG: return "Jacobi eigensolver reached its sweep limit";
+        case MEPI_ERR_NONHERM: return "H(R) is not Hermitian (H(-R) != H(R)^dag or -R missing)";
+        case MEPI_ERR_NONFINITE: return "NaN or Inf in the model";
+        default: return "unknown status";
+    }
+}
+
+int mepi_create(mepi_ctx** out, const mepi_model* m) {
+    if (!out || !m) return MEPI_ERR_ARG;
+    *out = nullptr;
+    if (m->n_wf <= 0 || m->n_wf > kMaxN || m->n_R <= 0 || !m->R_frac || !m->H) return MEPI_ERR_ARG;
+    if (m->semantics != MEPI_SEM_REF && m->semantics != MEPI_SEM_PAPER) return MEPI_ERR_ARG;
+    if (!(m->kubo_tol >= 0.0)) return MEPI_ERR_ARG;
+    const int N = m->n_wf, nR = m->n_R;
+    const size_t NN = (size_t)N * N;
+    if (!finite_all(m->R_frac, 3 * (size_t)nR) || !finite_all(m->H, 2 * NN * nR) || !finite_all(m->a_latt, 9))
+        return MEPI_ERR_NONFINITE;
+    if (m->r && !finite_all(m->r, 6 * NN * nR)) return MEPI_ERR_NONFINITE;
+    if (m->wf_centers && !finite_all(m->wf_centers, 3 * (size_t)N)) return MEPI_ERR_NONFINITE;
+    // Hermiticity: H(n,m,-R) = conj(H(m,n,R))
+    double hmax = 0;
+    for (size_t i = 0; i < 2 * NN * nR; ++i) hmax = std::max(hmax, std::fabs(m->H[i]));
+    const double htol = 1e-6 * hmax + 1e-9;
+    for (int r = 0; r < nR; ++r) {
+        int rm = -1;
+        for (int s = 0; s < nR && rm < 0; ++s) {
+            bool eq = true;
+            for (int i = 0; i < 3; ++i) eq = eq && std::fabs(m->R_frac[3 * s + i] + m->R_frac[3 * r + i]) <= 1e-9;
+            if (eq) rm = s;
+        }
+        if (rm < 0) return MEPI_ERR_NONHERM;
+        for (int a = 0; a < N; ++a)
+            for (int b = 0; b < N; ++b) {
+                const double* x = m->H + 2 * (a + N * b + NN * r);
+                const double* y = m->H + 2 * (b + N * a + NN * rm);
+                if (std::fabs(x[0] - y[0]) > htol || std::fabs(x[1] + y[1]) > htol) return MEPI_ERR_NONHERM;
+            }
+    }
+    int dev_count = 0;
+    if (cudaGetDeviceCount(&dev_count) != cudaSuccess || dev_count <= 0) {
+        cudaGetLastError();
+        return MEPI_ERR_CUDA;
+    }
+    mepi_ctx* ctx = new (std::nothrow) mepi_ctx();
+    if (!ctx) return MEPI_ERR_NOMEM;
+    auto fail = [&](int code) {
+        mepi_destroy(ctx);
+        return code;
+    };
+    if (cudaGetDevice(&ctx->device) != cudaSuccess) return fail(MEPI_ERR_CUDA);
+    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) return fail(MEPI_ERR_CUDA);
+    ctx->N = N;
+    ctx->nR = nR;
+    ctx->nb = m->r ? 10 : 4;
+    std::memcpy(ctx->a_latt, m->a_latt, sizeof(ctx->a_latt));
+    // derivative weights: dR_cart = matmul(a_latt, dR) or 2 pi dR
+    double C[9];
+    for (int a = 0; a < 3; ++a)
+        for (int j = 0; j < 3; ++j) C[a * 3 + j] = m->use_cart_velo ? m->a_latt[a + 3 * j] : (a == j ? 2.0 * kPi : 0.0);
+    // Fourier stack
+    const int nb = ctx->nb;
+    std::vector<cplx<double>> S;
+    try {
+        S.resize((size_t)nR * NN * nb);
+    } catch (...) {
+        return fail(MEPI_ERR_NOMEM);
+    }
+    const int qa[3] = {0, 0, 1}, qb[3] = {1, 2, 2};
+    for (int r = 0; r < nR; ++r) {
+        double CR[3];
+        for (int a = 0; a < 3; ++a)
+            CR[a] = C[a * 3 + 0] * m->R_frac[3 * r] + C[a * 3 + 1] * m->R_frac[3 * r + 1] + C[a * 3 + 2] * m->R_frac[3 * r + 2];
+        for (int n = 0; n < N; ++n)
+            for (int mm = 0; mm < N; ++mm) {
+                cplx<double>* s = &S[((size_t)r * NN + n * N + mm) * nb];
+                const double* h = m->H + 2 * (n + (size_t)N * mm + NN * r);
+                cplx<double> H = mk(h[0], h[1]);
+                s[0] = H;
+                for (int a = 0; a < 3; ++a) s[1 + a] = CR[a] * H;
+                if (m->r) {
+                    cplx<double> rv[3];
+                    for (int b = 0; b < 3; ++b) {
+                        const double* x = m->r + 2 * (b + 3 * (n + (size_t)N * (mm + (size_t)N * r)));
+                        rv[b] = mk(x[0], x[1]);
+                        s[4 + b] = rv[b];
+                    }
+                    for (int q = 0; q < 3; ++q) s[7 + q] = CR[qa[q]] * rv[qb[q]] - CR[qb[q]] * rv[qa[q]];
+                }
+            }
+    }
+    const char* simt_env = std::getenv("MEPI_FT_SIMT");
+    ctx->ft_simt_only = simt_env && simt_env[0] == '1';
+    std::vector<double> Rh(3 * (size_t)nR);
+    std::memcpy(Rh.data(), m->R_frac, Rh.size() * sizeof(double));
+    if (ctx->S.ensure(S.size() * sizeof(cplx<double>)) != cudaSuccess) return fail(MEPI_ERR_NOMEM);
+    if (ctx->R.ensure(Rh.size() * sizeof(double)) != cudaSuccess) return fail(MEPI_ERR_NOMEM);
+    if (cudaMemcpy(ctx->S.p, S.data(), S.size() * sizeof(cplx<double>), cudaMemcpyHostToDevice) != cudaSuccess)
+        return fail(MEPI_ERR_CUDA);
+    ctx->h2d += S.size() * sizeof(cplx<double>) + Rh.size() * sizeof(double);
+    ctx->S_host.swap(S);
+    if (cudaMemcpy(ctx->R.p, Rh.data(), Rh.size() * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess)
+        return fail(MEPI_ERR_CUDA);
+    if (m->wf_centers) {
+        if (ctx->tau.ensure(3 * (size_t)N * sizeof(double)) != cudaSuccess) return fail(MEPI_ERR_NOMEM);
+        if (cudaMemcpy(ctx->tau.p, m->wf_centers, 3 * (size_t)N * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess)
+            return fail(MEPI_ERR_CUDA);
+        ctx->h2d += 3 * (size_t)N * sizeof(double);
+    }
+    DevModel& d = ctx->dm;
+    d.N = N;
+    d.nR = nR;
+    d.nb = nb;
+    d.has_r = m->r ? 1 : 0;
+    d.has_tau = m->wf_centers ? 1 : 0;
+    d.semantics = m->semantics;
+    d.do_gauge = m->do_gauge_trafo ? 1 : 0;
+    d.kubo_tol = m->kubo_tol;
+    std::memcpy(d.C, C, sizeof(C));
+    d.S = ctx->S.as<cplx<double>>();
+    d.R = ctx->R.as<double>();
+    d.tau = m->wf_centers ? ctx->tau.as<double>() : nullptr;
+    *out = ctx;
+    return MEPI_OK;
+}
+
+int mepi_run(mepi_ctx* ctx, const mepi_job* job, mepi_acc* out) {
+    if (!ctx || !job || !out) return MEPI_ERR_ARG;
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return MEPI_ERR_CUDA;
+    try {
+        return run_impl(ctx, job, out);
+    } catch (const std::bad_alloc&) {
+        return MEPI_ERR_NOMEM;
+    } catch (...) {
+        return MEPI_ERR_CUDA;
+    }
+}
+
+int mepi_interp_k(mepi_ctx* ctx, int32_t precision, int64_t n_k, const double* kpts, double* en_k, double* V_ka,
+                  double* A_diag, double* Om_diag) {
+    if (!ctx || n_k < 0 || (n_k > 0 && (!kpts || !en_k || !V_ka))) return MEPI_ERR_ARG;
+    if (precision != MEPI_PREC_FP64 && precision != MEPI_PREC_MIXED) return MEPI_ERR_ARG;
+    if (n_k == 0) return MEPI_OK;
+    if (!finite_all(kpts, 3 * (size_t)n_k)) return MEPI_ERR_ARG;
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return MEPI_ERR_CUDA;
+    try {
+        const int N = ctx->N;
+        const size_t NN = (size_t)N * N;
+        const bool fp64 = precision == MEPI_PREC_FP64;
+        const int64_t chunk = std::min<int64_t>(n_k, 4096);
+        int rc = fp64 ? ensure_chunk<double>(ctx, chunk) : ensure_chunk<float>(ctx, chunk);
+        if (rc) return rc;
+        const size_t esz = fp64 ? sizeof(double) : sizeof(float);
+        CKM(ctx->ODH.ensure(chunk * 3 * N * 2 * esz));
+        CKM(ctx->kpts.ensure(n_k * 3 * sizeof(double)));
+        CKM(ctx->counters.ensure(4 * sizeof(int)));
+        CK(cudaMemsetAsync(ctx->counters.p, 0, 4 * sizeof(int), ctx->stream));
+        CK(cudaMemcpyAsync(ctx->kpts.p, kpts, n_k * 3 * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+        ctx->ev_used = 0;
+        std::vector<double> hE, hV, hHA, hO;
+        for (int64_t c0 = 0; c0 < n_k; c0 += chunk) {
+            const int64_t cn = std::min(chunk, n_k - c0);
+            KRange kr{0, 1, cn, nullptr, ctx->kpts.as<double>() + 3 * c0, {1, 1, 1}};
+            if (fp64)
+                rc = run_chunk<double>(ctx, kr, nullptr, 0, 0.0, false, false, ctx->ODH.as<cplx<double>>());
+            else
+                rc = run_chunk<float>(ctx, kr, nullptr, 0, 0.0, false, false, ctx->ODH.as<cplx<float>>());
+            if (rc) return rc;
+            // copy back and convert to double
+            std::vector<unsigned char> bE(cn * N * esz), bV(cn * 3 * NN * 2 * esz), bHA(cn * 6 * NN * 2 * esz),
+                bO(cn * 3 * N * 2 * esz);
+            CK(cudaMemcpyAsync(bE.data(), ctx->E.p, bE.size(), cudaMemcpyDeviceToHost, ctx->stream));
+            CK(cudaMemcpyAsync(bV.data(), ctx->V.p, bV.size(), cudaMemcpyDeviceToHost, ctx->stream));
+            CK(cudaMemcpyAsync(bHA.data(), ctx->HA.p, bHA.size(), cudaMemcpyDeviceToHost, ctx->stream));
+            CK(cudaMemcpyAsync(bO.data(), ctx->ODH.p, bO.size(), cudaMemcpyDeviceToHost, ctx->stream));
+            CK(cudaStreamSynchronize(ctx->stream));
+            auto conv = [&](const std::vector<unsigned char>& b, std::vector<double>& dst) {
+                size_t n = b.size() / esz;
+                size_t off = dst.size();
+                dst.resize(off + n);
+                if (fp64) std::memcpy(dst.data() + off, b.data(), b.size());
+                else {
+                    const float* f = reinterpret_cast<const float*>(b.data());
+                    for (size_t i = 0; i < n; ++i) dst[off + i] = f[i];
+                }
+            };
+            conv(bE, hE);
+            conv(bV, hV);
+            conv(bHA, hHA);
+            conv(bO, hO);
+        }
+        int hc[4];
+        CK(cudaMemcpy(hc, ctx->counters.p, sizeof(hc), cudaMemcpyDeviceToHost));
+        if (ctx->tc.err) {
+            int terr = 0;
+            CK(cudaMemcpy(&terr, ctx->tc.err, sizeof(int), cudaMemcpyDeviceToHost));
+            if (terr) return MEPI_ERR_CUDA;
+        }
+        // scatter into the Fortran layouts
+        for (int64_t k = 0; k < n_k; ++k) {
+            for (int n = 0; n < N; ++n) en_k[k * N + n] = hE[k * N + n];
+            for (int a = 0; a < 3; ++a)
+                for (int n = 0; n < N; ++n)
+                    for (int mm = 0; mm < N; ++mm) {
+                        size_t src = 2 * (((size_t)k * 3 + a) * NN + n * N + mm);
+                        size_t dst = 2 * (a + 3 * (n + (size_t)N * (mm + (size_t)N * k)));
+                        V_ka[dst] = hV[src];
+                        V_ka[dst + 1] = hV[src + 1];
+                    }
+            if (A_diag)
+                for (int n = 0; n < N; ++n)
+                    for (int c = 0; c < 3; ++c) {
+                        size_t src = 2 * (((size_t)k * 6 + 3 + c) * NN + n * N + n);
+                        size_t dst = 2 * (c + 3 * (n + (size_t)N * k));
+                        A_diag[dst] = hHA[src];
+                        A_diag[dst + 1] = hHA[src + 1];
+                    }
+            if (Om_diag) {
+                const int qa[3] = {0, 0, 1}, qb[3] = {1, 2, 2};
+                for (int n = 0; n < N; ++n) {
+                    double om[3][3][2];
+                    std::memset(om, 0, sizeof(om));
+                    for (int q = 0; q < 3; ++q) {
+                        size_t src = 2 * (((size_t)k * 3 + q) * N + n);
+                        double re = hO[src], im = hO[src + 1];
+                        om[qa[q]][qb[q]][0] = re;
+                        om[qa[q]][qb[q]][1] = im;
+                        om[qb[q]][qa[q]][0] = -re;
+                        om[qb[q]][qa[q]][1] = -im;
+                    }
+                    for (int a = 0; a < 3; ++a)
+                        for (int b = 0; b < 3; ++b) {
+                            size_t dst = 2 * (a + 3 * (b + 3 * (n + (size_t)N * k)));
+                            Om_diag[dst] = om[a][b][0];
+                            Om_diag[dst + 1] = om[a][b][1];
+                        }
+                }
+            }
+        }
+        if (fp64 && hc[1] > 0) return MEPI_ERR_EIG;
+        return MEPI_OK;
+    } catch (const std::bad_alloc&) {
+        return MEPI_ERR_NOMEM;
+    } catch (...) {
+        return MEPI_ERR_CUDA;
+    }
+}
+
+int mepi_get_timing(const mepi_ctx* ctx, mepi_timing* t) {
+    if (!ctx || !t) return MEPI_ERR_ARG;
+    *t = ctx->timing;
+    return MEPI_OK;
+}
+
+int mepi_destroy(mepi_ctx* ctx) {
+    if (!ctx) return MEPI_OK;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    for (DevBuf* b : {&ctx->S, &ctx->R, &ctx->tau, &ctx->W, &ctx->E, &ctx->U, &ctx->HA, &ctx->OD, &ctx->V, &ctx->CSV,
+                      &ctx->ODH, &ctx->flags, &ctx->klist, &ctx->kpts, &ctx->partials, &ctx->out, &ctx->counters})
+        b->release();
+    for (auto& ev : ctx->events) {
+        cudaEventDestroy(ev.a);
+        cudaEventDestroy(ev.b);
+    }
+    if (ctx->h_flags) cudaFreeHost(ctx->h_flags);
+    tc_plan_free(ctx->tc);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return MEPI_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,130 @@
+// Internal declarations shared by the CUDA translation units of libmepi_gb300.
+//
+// Device data layout (C order, matrices row-major, element (n,m) at n*N+m):
+//   S stack      S[R][pair][blk]        complex<double>, pair = n*N+m,
+//                blk 0: H(R); 1..3: (C R)_a H(R); 4..6: r_a(R);
+//                7..9: (C R)_a r_b(R) - (C R)_b r_a(R) for (a,b) = (x,y),(x,z),(y,z)
+//                with C = a_latt (use_cart_velo) or 2*pi*I; 4 blocks without r(R).
+//   W blocks     W[k][blk][n][m]        complex<T>, the Wannier-gauge H, H_a, A_a,
+//                Omega_q per k-point after the tau phase epilogue.
+//   E, U         E[k][n] ascending, U[k][i][n] = component i of eigenvector n.
+//   HA           HA[k][6][n][m]          complex<T>: Hbar_a (a=0..2), Abar_a.
+//   OD           OD[k][3][n]             complex<T>: diag(U^dag Omega_q U).
+//   V            V[k][3][n][m]           complex<T>: velocity matrices.
+//   CSV          CSV[k][n]               T: 0.5 Re(A_nn . om_vect_n) per band.
+//   partials     per-CTA FP64 accumulators reduced in a fixed order.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace mepi {
+
+constexpr double kPi = 3.14159265358979323846264338327950288;
+constexpr double kAuToEv = 27.211385;                    // src/constants.f90:19
+constexpr double kKbEhK = 8.6173303e-5 / 27.211385;      // src/constants.f90:22
+constexpr double kMinTemp = 1e-2;                        // src/statistics.f90:32
+constexpr int kMaxN = 64;                                // largest n_wf supported
+
+template <typename T> struct cplx { T re, im; };
+
+template <typename T> __host__ __device__ __forceinline__ cplx<T> mk(T r, T i) { cplx<T> c; c.re = r; c.im = i; return c; }
+template <typename T> __host__ __device__ __forceinline__ cplx<T> operator+(cplx<T> a, cplx<T> b) { return mk(a.re + b.re, a.im + b.im); }
+template <typename T> __host__ __device__ __forceinline__ cplx<T> operator-(cplx<T> a, cplx<T> b) { return mk(a.re - b.re, a.im - b.im); }
+template <typename T> __host__ __device__ __forceinline__ cplx<T> operator*(cplx<T> a, cplx<T> b) {
+    return mk(a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re);
+}
+template <typename T> __host__ __device__ __forceinline__ cplx<T> operator*(T s, cplx<T> a) { return mk(s * a.re, s * a.im); }
+template <typename T> __host__ __device__ __forceinline__ cplx<T> conjg(cplx<T> a) { return mk(a.re, -a.im); }
+// a * conj(b)
+template <typename T> __host__ __device__ __forceinline__ cplx<T> mul_cj(cplx<T> a, cplx<T> b) {
+    return mk(a.re * b.re + a.im * b.im, a.im * b.re - a.re * b.im);
+}
+// conj(a) * b
+template <typename T> __host__ __device__ __forceinline__ cplx<T> cj_mul(cplx<T> a, cplx<T> b) {
+    return mk(a.re * b.re + a.im * b.im, a.re * b.im - a.im * b.re);
+}
+// acc += a * b
+template <typename T> __host__ __device__ __forceinline__ void fma_c(cplx<T>& acc, cplx<T> a, cplx<T> b) {
+    acc.re = fma(a.re, b.re, acc.re); acc.re = fma(-a.im, b.im, acc.re);
+    acc.im = fma(a.re, b.im, acc.im); acc.im = fma(a.im, b.re, acc.im);
+}
+// acc += conj(a) * b
+template <typename T> __host__ __device__ __forceinline__ void fma_cjc(cplx<T>& acc, cplx<T> a, cplx<T> b) {
+    acc.re = fma(a.re, b.re, acc.re); acc.re = fma(a.im, b.im, acc.re);
+    acc.im = fma(a.re, b.im, acc.im); acc.im = fma(-a.im, b.re, acc.im);
+}
+template <typename T> __host__ __device__ __forceinline__ cplx<T> times_i(cplx<T> a) { return mk(-a.im, a.re); }
+template <typename T> __host__ __device__ __forceinline__ T abs2(cplx<T> a) { return a.re * a.re + a.im * a.im; }
+
+// Which k-points a launch covers: k = list ? list[i] : k_begin + i * k_stride.
+struct KRange {
+    int64_t k_begin, k_stride, count;
+    const int64_t* list;     // device pointer or nullptr
+    const double* kpts;      // device (count, 3) explicit k-points, or nullptr
+    int32_t mp[3];
+};
+
+__device__ __forceinline__ int64_t k_of(const KRange& kr, int64_t i) {
+    return kr.list ? kr.list[i] : kr.k_begin + i * kr.k_stride;
+}
+
+// Monkhorst-Pack point, src/k_space.f90:351-375 (kx fastest, 1-based q).
+__device__ __forceinline__ void mp_kpt(const int32_t mp[3], int64_t ki, double k[3]) {
+    int64_t q0 = ki % mp[0] + 1;
+    int64_t q1 = (ki / mp[0]) % mp[1] + 1;
+    int64_t q2 = ki / ((int64_t)mp[0] * mp[1]) + 1;
+    k[0] = (2.0 * (double)q0 - (double)mp[0] - 1.0) / (2.0 * (double)mp[0]);
+    k[1] = (2.0 * (double)q1 - (double)mp[1] - 1.0) / (2.0 * (double)mp[1]);
+    k[2] = (2.0 * (double)q2 - (double)mp[2] - 1.0) / (2.0 * (double)mp[2]);
+}
+
+// Model constants the epilogues need, in constant-size device structs.
+struct DevModel {
+    int N, nR, nb;            // n_wf, n_R, stack blocks (10 with r(R), 4 without)
+    int has_r, has_tau, semantics, do_gauge;
+    double kubo_tol;
+    double C[9];              // derivative weight matrix, row-major C[a*3+j]
+    const cplx<double>* S;    // S stack (nR, N*N, nb)
+    const double* R;          // R_frac (nR, 3)
+    const double* tau;        // (N, 3) or nullptr
+};
+
+struct JobDev {
+    int nE, nval, do_ahc, do_mep, do_kubo;
+    double T_kelvin;
+    const double* ef;         // device (nE)
+};
+
+// Layout of one CTA's FP64 accumulator slice.
+struct AccLayout {
+    int nE, nval;
+    __host__ __device__ int ne_off() const { return 0; }
+    __host__ __device__ int ahc_off() const { return nE; }
+    __host__ __device__ int kic_off() const { return nE + 9 * nE; }
+    __host__ __device__ int klc_off() const { return nE + 18 * nE; }
+    __host__ __device__ int kcs_off() const { return nE + 27 * nE; }
+    __host__ __device__ int mic_off() const { return nE + 36 * nE; }
+    __host__ __device__ int mlc_off() const { return nE + 36 * nE + 9 * nval; }
+    __host__ __device__ int mcs_off() const { return nE + 36 * nE + 18 * nval; }
+    __host__ __device__ int size() const { return nE + 36 * nE + 27 * nval; }
+};
+
+// ---- host launchers (one per translation unit) ----
+template <typename T>
+cudaError_t launch_ft_simt(const DevModel& m, const KRange& kr, cplx<T>* W, cudaStream_t s);
+template <typename T>
+cudaError_t launch_eig(int N, int64_t nk, const cplx<T>* W, int nbW, T* E, cplx<T>* U, int max_sweeps,
+                       int* sweeps_max, int* flag_cap, double degen_gap, int* redo_flag, cudaStream_t s);
+template <typename T>
+cudaError_t launch_rot(const DevModel& m, int64_t nk, const cplx<T>* W, const cplx<T>* U, cplx<T>* HA,
+                       cplx<T>* OD, cudaStream_t s);
+template <typename T>
+cudaError_t launch_gauge(const DevModel& m, int64_t nk, const T* E, const cplx<T>* HA, const cplx<T>* OD,
+                         cplx<T>* V, T* CSV, cplx<T>* ODH, cudaStream_t s);
+template <typename T>
+cudaError_t launch_bandsum(const DevModel& m, const JobDev& j, int64_t nk, const T* E, const cplx<T>* V,
+                           const T* CSV, const int* skip, double* partials, int n_cta, cudaStream_t s);
+cudaError_t launch_reduce(const double* partials, int n_cta, int size, double* out, cudaStream_t s);
+int bandsum_ctas();
+
+}  // namespace mepi

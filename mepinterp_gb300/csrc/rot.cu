@@ -1,0 +1,107 @@
+// W -> Hbar gauge rotation of rotate_gauge (src/wann_interp.f90:502-550):
+//     Hbar_a = U^dag H_a U,   Abar_a = U^dag A_a U   (a = x,y,z; D1 position:
+//     the connection is rotated from A_a itself, not from the stale buffer the
+//     reference reuses at :531-533),
+// and only the band diagonal of U^dag Omega_q U for the three independent
+// curvature components -- the band sums consume no other part of Omega
+// (src/mep_niu.f90:35, src/kubo_mep.f90:35), so the 54 zgemm per k of
+// curv_gaugeTrafo collapse to 3 diagonal-only rotations here plus O(N^2)
+// commutator diagonals in the gauge kernel.
+//
+// One k-point per CTA: U and the operand are staged in shared memory and each
+// product is an N x N x N complex contraction spread over the CTA's threads
+// (thread (i, j) reads a broadcast row element and a contiguous column run).
+// Without the gauge transformation the kernel copies the W-gauge blocks.
+#include "mepi_internal.cuh"
+
+namespace mepi {
+
+namespace {
+
+template <typename T>
+__global__ void __launch_bounds__(256) rot_kernel(DevModel m, const cplx<T>* __restrict__ W,
+                                                  const cplx<T>* __restrict__ Ug, cplx<T>* __restrict__ HA,
+                                                  cplx<T>* __restrict__ OD) {
+    extern __shared__ unsigned char smem_raw[];
+    const int N = m.N, NN = N * N;
+    cplx<T>* Us = reinterpret_cast<cplx<T>*>(smem_raw);
+    cplx<T>* Xs = Us + NN;
+    cplx<T>* Ts = Xs + NN;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const int64_t k = blockIdx.x;
+    const int nbW = m.nb;
+    const cplx<T>* Wk = W + (size_t)k * nbW * NN;
+    const int nmat = m.has_r ? 6 : 3;
+    cplx<T>* HAk = HA + (size_t)k * 6 * NN;
+
+    if (!m.do_gauge) {
+        for (int j = 0; j < nmat; ++j)
+            for (int e = tid; e < NN; e += nt) HAk[(size_t)j * NN + e] = Wk[(size_t)(1 + j) * NN + e];
+        if (m.has_r)
+            for (int q = 0; q < 3; ++q)
+                for (int n = tid; n < N; n += nt) OD[((size_t)k * 3 + q) * N + n] = Wk[(size_t)(7 + q) * NN + n * N + n];
+        return;
+    }
+    for (int e = tid; e < NN; e += nt) Us[e] = Ug[(size_t)k * NN + e];
+    // blocks 1..3 (H_a) and 4..6 (A_a): full rotation
+    for (int j = 0; j < nmat; ++j) {
+        __syncthreads();
+        for (int e = tid; e < NN; e += nt) Xs[e] = Wk[(size_t)(1 + j) * NN + e];
+        __syncthreads();
+        // T = X U
+        for (int e = tid; e < NN; e += nt) {
+            int i = e / N, c = e % N;
+            cplx<T> acc = mk((T)0, (T)0);
+            for (int l = 0; l < N; ++l) fma_c(acc, Xs[i * N + l], Us[l * N + c]);
+            Ts[e] = acc;
+        }
+        __syncthreads();
+        // Y = U^dag T
+        for (int e = tid; e < NN; e += nt) {
+            int i = e / N, c = e % N;
+            cplx<T> acc = mk((T)0, (T)0);
+            for (int l = 0; l < N; ++l) fma_cjc(acc, Us[l * N + i], Ts[l * N + c]);
+            HAk[(size_t)j * NN + e] = acc;
+        }
+    }
+    if (!m.has_r) return;
+    // blocks 7..9 (Omega_q): diagonal of U^dag Omega_q U only
+    for (int q = 0; q < 3; ++q) {
+        __syncthreads();
+        for (int e = tid; e < NN; e += nt) Xs[e] = Wk[(size_t)(7 + q) * NN + e];
+        __syncthreads();
+        for (int e = tid; e < NN; e += nt) {
+            int i = e / N, c = e % N;
+            cplx<T> acc = mk((T)0, (T)0);
+            for (int l = 0; l < N; ++l) fma_c(acc, Xs[i * N + l], Us[l * N + c]);
+            Ts[e] = acc;
+        }
+        __syncthreads();
+        for (int n = tid; n < N; n += nt) {
+            cplx<T> acc = mk((T)0, (T)0);
+            for (int l = 0; l < N; ++l) fma_cjc(acc, Us[l * N + n], Ts[l * N + n]);
+            OD[((size_t)k * 3 + q) * N + n] = acc;
+        }
+    }
+}
+
+}  // namespace
+
+template <typename T>
+cudaError_t launch_rot(const DevModel& m, int64_t nk, const cplx<T>* W, const cplx<T>* U, cplx<T>* HA, cplx<T>* OD,
+                       cudaStream_t s) {
+    if (nk <= 0) return cudaSuccess;
+    size_t smem = 3 * (size_t)m.N * m.N * sizeof(cplx<T>);
+    cudaError_t e = cudaFuncSetAttribute(rot_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int threads = m.N <= 16 ? 128 : 256;
+    rot_kernel<T><<<(unsigned)nk, threads, smem, s>>>(m, W, U, HA, OD);
+    return cudaGetLastError();
+}
+
+template cudaError_t launch_rot<double>(const DevModel&, int64_t, const cplx<double>*, const cplx<double>*,
+                                        cplx<double>*, cplx<double>*, cudaStream_t);
+template cudaError_t launch_rot<float>(const DevModel&, int64_t, const cplx<float>*, const cplx<float>*, cplx<float>*,
+                                       cplx<float>*, cudaStream_t);
+
+}  // namespace mepi

@@ -1,0 +1,118 @@
+"""CPU checks of the C ABI boundary: the library builds, loads, exports every
+function include/mepi.h declares, its ctypes mirror has the header's struct
+layouts, and argument validation answers before any device work."""
+import ctypes as C
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+from mepinterp_gb300 import api, build
+from mepinterp_gb300.generator import random_tb_model
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "mepi.h")
+
+
+@pytest.fixture(scope="module")
+def lib():
+    build.build()
+    return api.load_library()
+
+
+def header_functions():
+    txt = open(HEADER).read()
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?\w+\s*\*?\s*(mepi_\w+)\s*\(", txt, flags=re.M)))
+
+
+def test_exports_every_declared_symbol(lib):
+    names = header_functions()
+    assert {"mepi_create", "mepi_run", "mepi_destroy", "mepi_strerror", "mepi_interp_k"} <= set(names)
+    for n in names:
+        assert hasattr(lib, n), n
+
+
+def test_struct_layouts_match_header(tmp_path):
+    """sizeof/offsetof from a C compile of mepi.h equal the ctypes mirror's."""
+    fields = {"mepi_model": api.MepiModel, "mepi_job": api.MepiJob, "mepi_acc": api.MepiAcc,
+              "mepi_timing": api.MepiTiming}
+    src = ['#include <stdio.h>', '#include <stddef.h>', '#include "mepi.h"', "int main(void){"]
+    for cname, cls in fields.items():
+        src.append(f'printf("{cname} %zu\\n", sizeof({cname}));')
+        for f, _ in cls._fields_:
+            src.append(f'printf("{cname}.{f} %zu\\n", offsetof({cname}, {f}));')
+    src.append("return 0;}")
+    c = tmp_path / "probe.c"
+    c.write_text("\n".join(src))
+    exe = tmp_path / "probe"
+    subprocess.check_call(["gcc", "-I", os.path.join(ROOT, "include"), str(c), "-o", str(exe)])
+    out = dict(line.split() for line in subprocess.check_output([str(exe)]).decode().splitlines())
+    for cname, cls in fields.items():
+        assert int(out[cname]) == C.sizeof(cls), cname
+        for f, _ in cls._fields_:
+            assert int(out[f"{cname}.{f}"]) == getattr(cls, f).offset, (cname, f)
+
+
+def test_strerror_and_version(lib):
+    for s in range(7):
+        assert lib.mepi_strerror(s)
+    assert b"sm_103a" in lib.mepi_version()
+
+
+def _create(lib, model, mutate=None):
+    bufs = api.fortran_model_arrays(model)
+    m = api.make_mepi_model(model, bufs)
+    if mutate:
+        mutate(m, bufs)
+    h = C.c_void_p()
+    rc = lib.mepi_create(C.byref(h), C.byref(m))
+    if rc == 0:
+        lib.mepi_destroy(h)
+    return rc
+
+
+def test_create_rejects_bad_arguments(lib):
+    model = random_tb_model(n_wf=8, r_max=1, seed=1)
+    assert lib.mepi_create(None, None) == api.ERR_ARG
+
+    def zero_n(m, b):
+        m.n_wf = 0
+    assert _create(lib, model, zero_n) == api.ERR_ARG
+
+    def too_big(m, b):
+        m.n_wf = 65
+    assert _create(lib, model, too_big) == api.ERR_ARG
+
+    def bad_sem(m, b):
+        m.semantics = 7
+    assert _create(lib, model, bad_sem) == api.ERR_ARG
+
+
+def test_create_rejects_nan_and_non_hermitian(lib):
+    model = random_tb_model(n_wf=8, r_max=1, seed=1)
+    bad = random_tb_model(n_wf=8, r_max=1, seed=1)
+    bad.H = bad.H.copy()
+    bad.H[3, 1, 2] = np.nan
+    assert _create(lib, bad) == api.ERR_NONFINITE
+    nh = random_tb_model(n_wf=8, r_max=1, seed=1)
+    nh.H = nh.H.copy()
+    nh.H[5, 0, 1] += 0.01
+    assert _create(lib, nh) == api.ERR_NONHERM
+    half = random_tb_model(n_wf=8, r_max=1, seed=1)
+    keep = [i for i in range(half.n_R) if tuple(half.R_frac[i]) != (1.0, 0.0, 0.0)]
+    half.R_frac, half.H, half.r = half.R_frac[keep], half.H[keep], half.r[keep]
+    assert _create(lib, half) == api.ERR_NONHERM
+    del model
+
+
+def test_no_gpu_fails_loudly(lib):
+    """Without a CUDA device the library refuses (no CPU fallback exists)."""
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    model = random_tb_model(n_wf=8, r_max=1, seed=1)
+    with pytest.raises(api.MepiError) as e:
+        api.Context(model)
+    assert e.value.status == api.ERR_CUDA

@@ -1,0 +1,199 @@
+"""GPU parity of the CUDA path (through the C ABI) against the CPU oracle.
+
+Tolerances (the plain form is all-FP64 and must match the reference's
+LAPACK-zheevd FP64 path):
+  eigenvalues                 1e-10 relative to max |E|
+  sigma_ab, MEP tensors       1e-8 relative to the largest entry of each tensor
+The mixed form (split-FP16 Fourier sums, FP32 per-k work, FP64 k-sums and FP64
+rerun of near-degenerate k-points) is held to 1e-6 relative on the k-summed
+tensors.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from mepinterp_gb300 import api
+from mepinterp_gb300.generator import random_tb_model, workload
+from oracle import ref_numpy as O
+
+pytestmark = pytest.mark.gpu
+
+KEYS = ["Ne_sum", "ahc", "mep_ic", "mep_lc", "mep_cs", "kubo_mep_ic", "kubo_mep_lc", "kubo_mep_cs"]
+GOLD = os.path.join(os.path.dirname(__file__), "golden", "femn.npz")
+E_TOL, SUM_TOL, MIXED_TOL = 1e-10, 1e-8, 1e-6
+
+
+def rel(a, b):
+    a, b = np.asarray(a, dtype=np.float64), np.asarray(b, dtype=np.float64)
+    scale = np.abs(b).max()
+    if scale == 0.0:
+        return float(np.abs(a).max())
+    return float(np.abs(a - b).max() / scale)
+
+
+def check_sums(gpu, ref, tol, keys=KEYS):
+    for k in keys:
+        r = rel(gpu[k], ref[k])
+        assert r < tol, f"{k}: rel err {r:.3e} (max |ref| {np.abs(ref[k]).max():.3e})"
+
+
+@pytest.fixture(scope="module")
+def model8():
+    return random_tb_model(n_wf=8, r_max=1, seed=1)
+
+
+def test_eigenvalues_fp64(gpu_lib, model8):
+    rng = np.random.default_rng(0)
+    kp = rng.uniform(-0.5, 0.5, size=(97, 3))
+    with api.Context(model8) as ctx:
+        E, V, A, Om = ctx.get_wann_interp(kp)
+    E2, U2, V2, A2, Om2 = O.interp_k(model8.as_dict(), kp)
+    assert np.abs(E - E2).max() <= E_TOL * np.abs(E2).max()
+    # gauge-invariant parts of the velocity: |V| and the band diagonal
+    idx = np.arange(8)
+    assert rel(np.abs(V), np.abs(V2)) < 1e-9
+    assert rel(V[:, :, idx, idx], V2[:, :, idx, idx]) < 1e-9
+    assert rel(A, A2[:, :, idx, idx]) < 1e-9
+    assert rel(Om, Om2[:, :, :, idx, idx]) < 1e-9
+    # V_i(n,m) V_j(m,n) products are gauge invariant
+    P = np.einsum("kinm,kjmn->kijnm", V, V)
+    P2 = np.einsum("kinm,kjmn->kijnm", V2, V2)
+    assert rel(P, P2) < 1e-9
+
+
+@pytest.mark.parametrize("with_r,tb,gauge,sem,cart", [
+    (True, True, True, "ref", False), (False, True, True, "ref", False), (True, False, True, "ref", False),
+    (True, True, False, "ref", False), (True, True, True, "paper", False), (True, True, True, "ref", True),
+])
+def test_kloop_fp64_modes(gpu_lib, with_r, tb, gauge, sem, cart):
+    m = random_tb_model(n_wf=8, r_max=1, seed=11, with_r=with_r, tb_convention=tb)
+    m.semantics, m.do_gauge_trafo, m.use_cart_velo = sem, gauge, cart
+    if cart:
+        m.a_latt = np.array([[5.0, 0.2, 0.1], [0.3, 4.5, 0.0], [0.1, 0.2, 6.0]])
+    job = dict(mp_grid=(6, 6, 6), ef_lst=np.array([-0.03, 0.0, 0.02]), T_kelvin=300.0, valence_bands=4)
+    ref = O.run(m.as_dict(), job)
+    got = api.run(m, job, precision=api.PREC_FP64)
+    assert got["n_k"] == ref["n_k"] == 216
+    check_sums(got, ref, SUM_TOL)
+
+
+def test_kloop_fp64_config1(gpu_lib):
+    """nWf=8, nR=27, 16^3 mesh, E_F=0, T=0 (the CPU-runnable configuration)."""
+    model, job = workload("tb8_r1_k16")
+    ref = O.run(model.as_dict(), job, batch=512)
+    got = api.run(model, job, precision=api.PREC_FP64, chunk_k=1000)
+    assert got["n_k"] == 4096
+    check_sums(got, ref, SUM_TOL)
+
+
+def test_kloop_fp64_nwf32_subset(gpu_lib):
+    """nWf=32, nR=343 model on a strided k subset of its 128^3 mesh."""
+    model, job = workload("tb32_r3_k128")
+    nk = 128 ** 3
+    stride = nk // 96 + 1
+    kidx = np.arange(0, nk, stride)
+    ref = O.run(model.as_dict(), job, k_indices=kidx, batch=16)
+    got = api.run(model, job, precision=api.PREC_FP64, k_begin=0, k_stride=stride)
+    assert got["n_k"] == kidx.size
+    check_sums(got, ref, SUM_TOL)
+
+
+def test_fermi_sweep_finite_T(gpu_lib):
+    m = random_tb_model(n_wf=12, r_max=2, decay=1.2, seed=21)
+    ef = np.linspace(-1.0, 1.0, 37) / O.AU_TO_EV
+    job = dict(mp_grid=(5, 5, 5), ef_lst=ef, T_kelvin=290.1, valence_bands=6)
+    ref = O.run(m.as_dict(), job)
+    got = api.run(m, job, precision=api.PREC_FP64)
+    check_sums(got, ref, SUM_TOL)
+    # the >= 64 Fermi-energy code path
+    ef2 = np.linspace(-1.5, 1.5, 101) / O.AU_TO_EV
+    job2 = dict(job, ef_lst=ef2)
+    check_sums(api.run(m, job2, precision=api.PREC_FP64), O.run(m.as_dict(), job2), SUM_TOL)
+
+
+@pytest.mark.parametrize("n_wf", [5, 16, 64])
+def test_odd_and_large_n(gpu_lib, n_wf):
+    m = random_tb_model(n_wf=n_wf + (n_wf % 2), r_max=1, seed=n_wf)
+    if n_wf % 2:  # odd band count: drop the last orbital
+        m.H = m.H[:, :n_wf, :n_wf]
+        m.r = m.r[:, :, :n_wf, :n_wf]
+        m.wf_centers = m.wf_centers[:n_wf]
+    job = dict(mp_grid=(3, 3, 3), ef_lst=[0.0], T_kelvin=0.0, valence_bands=n_wf // 2)
+    ref = O.run(m.as_dict(), job, batch=9)
+    got = api.run(m, job, precision=api.PREC_FP64)
+    check_sums(got, ref, SUM_TOL)
+
+
+def test_femn_golden_gpu(gpu_lib):
+    g = np.load(GOLD)
+    m = api.TBModel(R_frac=g["R_0p900"].astype(float), H=g["H_eV_0p900"] / O.AU_TO_EV,
+                    wf_centers=g["wf_centers"], a_latt=g["latt_0p900"])
+    job = dict(mp_grid=(32, 32, 32), ef_lst=[0.0], T_kelvin=0.0, valence_bands=4, do_mep=False, do_kubo=False)
+    got = api.run(m, job, precision=api.PREC_FP64)
+    _, vol = O.recip_latt(g["latt_0p900"])
+    s = got["ahc"][:, :, 0] / abs(vol * 32 ** 3)
+    gold = g["ahc_0p900"]
+    assert abs(s[0, 1] - gold[0, 1]) < 2e-3 * abs(gold[0, 1])
+    ref = O.run(dict(R_frac=m.R_frac, H=m.H, wf_centers=m.wf_centers, a_latt=m.a_latt), job, batch=1024)
+    check_sums(got, ref, SUM_TOL, keys=["ahc", "Ne_sum"])
+
+
+def test_k_partition_gpu(gpu_lib, model8):
+    job = dict(mp_grid=(8, 8, 8), ef_lst=[0.0], T_kelvin=0.0, valence_bands=4)
+    with api.Context(model8) as ctx:
+        full = ctx.core_worker_loc(job)
+        parts = [ctx.core_worker_loc(job, k_begin=r, k_stride=3) for r in range(3)]
+    assert sum(p["n_k"] for p in parts) == 512
+    for k in KEYS:
+        assert rel(sum(p[k] for p in parts), full[k]) < 1e-12
+
+
+def test_mixed_config1(gpu_lib):
+    model, job = workload("tb8_r1_k16")
+    ref = O.run(model.as_dict(), job, batch=512)
+    got = api.run(model, job, precision=api.PREC_MIXED)
+    assert got["n_k"] == 4096
+    check_sums(got, ref, MIXED_TOL)
+
+
+def test_mixed_fermi_sweep(gpu_lib):
+    m = random_tb_model(n_wf=12, r_max=2, decay=1.2, seed=21)
+    ef = np.linspace(-1.0, 1.0, 37) / O.AU_TO_EV
+    job = dict(mp_grid=(6, 6, 6), ef_lst=ef, T_kelvin=290.1, valence_bands=6)
+    ref = O.run(m.as_dict(), job)
+    got = api.run(m, job, precision=api.PREC_MIXED)
+    check_sums(got, ref, MIXED_TOL)
+
+
+def test_mixed_full_mesh_partition(gpu_lib):
+    """nWf=32 model on its full 128^3 mesh in the mixed form: two round-robin
+    'ranks' sum to the single run (size-independent property), and a strided
+    subset agrees with the FP64 path."""
+    model, job = workload("tb32_r3_k128")
+    with api.Context(model) as ctx:
+        full = ctx.core_worker_loc(job, precision=api.PREC_MIXED)
+        assert full["n_k"] == 128 ** 3
+        parts = [ctx.core_worker_loc(job, precision=api.PREC_MIXED, k_begin=r, k_stride=2) for r in range(2)]
+        for k in KEYS:
+            assert rel(parts[0][k] + parts[1][k], full[k]) < 1e-9, k
+        stride = 997
+        a = ctx.core_worker_loc(job, precision=api.PREC_MIXED, k_stride=stride)
+        b = ctx.core_worker_loc(job, precision=api.PREC_FP64, k_stride=stride)
+        check_sums(a, b, MIXED_TOL)
+
+
+def test_run_argument_errors(gpu_lib, model8):
+    with api.Context(model8) as ctx:
+        with pytest.raises(api.MepiError) as e:
+            ctx.core_worker_loc(dict(mp_grid=(0, 4, 4), ef_lst=[0.0], valence_bands=4))
+        assert e.value.status == api.ERR_ARG
+        with pytest.raises(api.MepiError) as e:
+            ctx.core_worker_loc(dict(mp_grid=(4, 4, 4), ef_lst=[0.0], valence_bands=9))
+        assert e.value.status == api.ERR_ARG
+        with pytest.raises(api.MepiError) as e:
+            ctx.core_worker_loc(dict(mp_grid=(4, 4, 4), ef_lst=[np.nan], valence_bands=4))
+        assert e.value.status == api.ERR_ARG
+        # still usable after rejected calls
+        ok = ctx.core_worker_loc(dict(mp_grid=(2, 2, 2), ef_lst=[0.0], valence_bands=4))
+        assert ok["n_k"] == 8
