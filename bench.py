@@ -1,0 +1,355 @@
+#!/usr/bin/env python
+"""Benchmark: k-points/s for AHE + MEP on the nWf=32 tight-binding model.
+
+Workload (one "step" = one pass of the k-loop over the whole mesh):
+  tb32_r3_k128 -- seeded random model with nWf = 32 (16 orbitals x spin),
+  R in {-3..3}^3 (nR = 343), hopping decay exp(-|R|/1.5), r(R) present,
+  tight-binding phase convention, 128^3 Monkhorst-Pack mesh (2,097,152 k),
+  E_F = 0, T = 0, valence_bands = 16; AHC + Niu MEP + Kubo MEP outputs.
+  Default form: mixed (split-FP16 tensor-core Fourier sums, FP32 per-k work,
+  FP64 k-sums and FP64 rerun of near-degenerate k-points).
+
+Arms:
+  (default)         the CUDA library through its C ABI; `value` times
+                    mepi_run with the model already resident on the GPU
+                    (CUDA events on the library's stream), `e2e` times the
+                    public API end to end from host buffers
+                    (mepi_create + mepi_run + mepi_destroy).
+  --impl reference  the reference's CPU algorithm (the C restatement in
+                    oracle/, OpenMP over all host threads) on a bounded
+                    sample of the same mesh each step.
+
+Prints one JSON line on rank 0.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "k-points/s for AHE+MEP, nWf=32"
+UNIT = "k-points/s"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    p.add_argument("--workload", default="tb32_r3_k128")
+    p.add_argument("--precision", choices=["mixed", "fp64"], default="mixed")
+    p.add_argument("--e2e-steps", type=int, default=2)
+    p.add_argument("--cpu-sample", type=int, default=0, help="k-points for the CPU baseline (0 = about 15 s)")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--k-stride", type=int, default=1,
+                   help="process every k-stride-th k-point of the mesh (small cases for profiling)")
+    p.add_argument("--fp64-check", type=int, default=65536,
+                   help="k-points of a strided subset on which the FP64 path is run for the error report (0 = off)")
+    return p.parse_args()
+
+
+def dist_setup():
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    local = int(os.environ.get("LOCAL_RANK", 0))
+    if world > 1:
+        # one GPU per rank: the CUDA library uses the first visible device
+        os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    return rank, world
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allreduce_max(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle-reason samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", "clocks_bench.csv")
+
+    def start(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=self.fh, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.fh.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        busy = [s for s in sm if s > 0.5 * (max(sm) if sm else 1)]
+        return {"sm_mhz": statistics.median(busy) if busy else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def flops_per_k(N, nR, nval, nE, has_r=True):
+    """Algorithmic real flops per k-point by stage (complex MAC = 8 flops)."""
+    nb = 10 if has_r else 4
+    r = 1 if has_r else 0
+    return {
+        "ft": 8.0 * nR * nb * N * N,
+        "eig": 80.0 / 3.0 * N ** 3,
+        "rot": 16.0 * N ** 3 * (3 + 3 * r) + 24.0 * N ** 3 * r,
+        "gauge": 180.0 * N * N,
+        "bandsum": 48.0 * N ** 3 + 48.0 * N * N * nval + 2.0 * 9 * N * (N + nE) * 4,
+    }
+
+
+def cpu_baseline(model, job, sample):
+    """The oracle's C restatement on all host threads over a strided sample."""
+    from oracle import ref_c
+    mp = job["mp_grid"]
+    nk = mp[0] * mp[1] * mp[2]
+    threads = os.cpu_count() or 1
+    if sample <= 0:
+        # calibrate: ~15 s of work
+        t0 = time.perf_counter()
+        ref_c.run(model.as_dict(), job, k_begin=0, k_count=threads, k_stride=nk // threads, nthreads=threads)
+        per_k = (time.perf_counter() - t0) / threads
+        sample = max(threads, int(15.0 / max(per_k * 1.0, 1e-9) * 1.0) // threads * threads)
+        sample = min(sample, nk)
+    stride = max(1, nk // sample)
+    t0 = time.perf_counter()
+    res = ref_c.run(model.as_dict(), job, k_begin=0, k_count=sample, k_stride=stride, nthreads=threads)
+    dt = time.perf_counter() - t0
+    return {"value": res["n_k"] / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{res['n_k']} k-points (every {stride}th of the {mp[0]}x{mp[1]}x{mp[2]} mesh), "
+                      f"{dt:.1f} s on {threads} threads"}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    from mepinterp_gb300.generator import workload
+    from oracle import ref_c
+    ref_c.build()
+    model, job = workload(args.workload)
+    mp = job["mp_grid"]
+    nk = mp[0] * mp[1] * mp[2]
+    threads = os.cpu_count() or 1
+    sample = args.cpu_sample if args.cpu_sample > 0 else 8 * threads
+    stride = max(1, nk // sample)
+    for _ in range(max(0, args.warmup)):
+        ref_c.run(model.as_dict(), job, k_begin=0, k_count=threads, k_stride=stride, nthreads=threads)
+    times = []
+    n_done = 0
+    for s in range(args.steps):
+        t0 = time.perf_counter()
+        res = ref_c.run(model.as_dict(), job, k_begin=s, k_count=sample, k_stride=stride, nthreads=threads)
+        times.append(time.perf_counter() - t0)
+        n_done += res["n_k"]
+    value = n_done / sum(times)
+    out = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded random tight-binding model)",
+        "config": {"workload": args.workload, "n_wf": 32, "n_R": 343, "mesh": list(mp),
+                   "sample_per_step": sample, "form": "reference CPU algorithm (C restatement, OpenMP over k)"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{sample} strided k-points per step of the {mp[0]}^3 mesh"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out))
+
+
+def run_gpu(args, rank, world):
+    import numpy as np
+    import torch
+    from mepinterp_gb300 import api
+    from mepinterp_gb300.generator import workload
+
+    model, job = workload(args.workload)
+    mp = job["mp_grid"]
+    ks = max(1, args.k_stride)
+    nk = (mp[0] * mp[1] * mp[2] + ks - 1) // ks
+    prec = api.PREC_MIXED if args.precision == "mixed" else api.PREC_FP64
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2 (129 MB)
+
+    ctx = api.Context(model)
+    for _ in range(max(args.warmup, 3)):
+        ctx.core_worker_loc(job, precision=prec, k_stride=ks)
+    # timed region: exactly K steps, L2 flushed before each one
+    clocks = ClockSampler()
+    barrier(world)
+    torch.cuda.synchronize()
+    clocks.start()
+    t_host0 = time.perf_counter()
+    run_ms = []
+    stage = {}
+    launches = 0
+    res = None
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        res = ctx.core_worker_loc(job, precision=prec, k_stride=ks)
+        t = ctx.timing()
+        run_ms.append(t["run_ms"])
+        for key in ("ft", "phase", "eig", "rot", "gauge", "bandsum", "reduce"):
+            stage.setdefault(key, [0.0, 0])
+            stage[key][0] += t[key + "_ms"]
+            stage[key][1] += t[key + "_launches"]
+            launches += t[key + "_launches"]
+    torch.cuda.synchronize()
+    t_host = time.perf_counter() - t_host0
+    barrier(world)
+    clk = clocks.stop()
+    dev_ms = allreduce_max(sum(run_ms), world)
+    value = world * nk * args.steps / (dev_ms * 1e-3)
+
+    # end to end through the public API with host buffers
+    e2e_times = []
+    h2d = d2h = 0
+    for _ in range(max(0, args.e2e_steps)):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        with api.Context(model) as c2:
+            c2.core_worker_loc(job, precision=prec, k_stride=ks)
+            t2 = c2.timing()
+        e2e_times.append(time.perf_counter() - t0)
+        h2d, d2h = t2["h2d_bytes"], t2["d2h_bytes"]
+    e2e_value = e2e_s = None
+    if e2e_times:
+        e2e_s = allreduce_max(statistics.median(e2e_times), world)
+        e2e_value = world * nk / e2e_s
+
+    # roofline of the dominant kernel (algorithmic flops / average launch time)
+    f = flops_per_k(model.n_wf, model.n_R, job["valence_bands"], len(job["ef_lst"]), model.r is not None)
+    stage_ms = {k: v[0] for k, v in stage.items()}
+    dom = max(("ft", "eig", "rot", "gauge", "bandsum"), key=lambda k: stage_ms.get(k, 0.0))
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    flops_per_launch = f[dom] * nk * args.steps / max(stage[dom][1], 1)
+    avg_launch_s = stage_ms[dom] * 1e-3 / max(stage[dom][1], 1)
+    achieved = flops_per_launch / avg_launch_s / 1e12
+    if dom == "ft" and prec == api.PREC_MIXED:
+        bound, peak = "tensor", peaks.get("bf16_tflops", 1900.0)
+        peak_src = "of measured" if "bf16_tflops" in peaks else "of fallback"
+    else:
+        # CUDA-core kernels: FP32 (mixed) / FP64 (plain) FMA pipes
+        bound = "tensor"
+        peak = peaks.get("bf16_tflops", 1900.0)
+        peak_src = "of measured bf16 tensor peak (this kernel runs on CUDA cores)"
+    roofline = {"bound": bound, "kernel": dom, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": achieved / peak, "peak_source": peak_src, "traffic": None,
+                "flops_per_launch": flops_per_launch, "avg_launch_ms": avg_launch_s * 1e3,
+                "stage_ms_per_step": {k: v / args.steps for k, v in stage_ms.items()}}
+
+    # error of this form against the FP64 path on a strided subset
+    err = None
+    if args.fp64_check > 0 and prec == api.PREC_MIXED:
+        stride = max(1, (mp[0] * mp[1] * mp[2]) // args.fp64_check)
+        a = ctx.core_worker_loc(job, precision=api.PREC_MIXED, k_stride=stride)
+        b = ctx.core_worker_loc(job, precision=api.PREC_FP64, k_stride=stride)
+        err = {"k_points": int(a["n_k"]), "k_stride": stride}
+        for key in ("ahc", "mep_ic", "mep_lc", "mep_cs", "kubo_mep_ic", "kubo_mep_lc", "kubo_mep_cs"):
+            x, y = np.asarray(a[key]), np.asarray(b[key])
+            scale = float(np.abs(y).max())
+            err[key] = float(np.abs(x - y).max() / scale) if scale > 0 else float(np.abs(x).max())
+        # sigma_xy and the MEP tensor (sum over valence bands of IC + LC + CS)
+        sxy = lambda r: r["ahc"][0, 1, 0]
+        mep = lambda r: (np.asarray(r["mep_ic"]) + np.asarray(r["mep_lc"]) + np.asarray(r["mep_cs"])).sum(-1)
+        err["sigma_xy"] = float(abs(sxy(a) - sxy(b)) / abs(sxy(b)))
+        err["mep_tensor"] = float(np.abs(mep(a) - mep(b)).max() / np.abs(mep(b)).max())
+    ctx.close()
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        try:
+            from oracle import ref_c
+            ref_c.build()
+            cpu = cpu_baseline(model, job, args.cpu_sample)
+        except Exception as exc:  # the baseline is reported, never required
+            cpu = {"value": None, "unit": UNIT, "error": str(exc)}
+
+    if rank == 0:
+        out = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": max(args.warmup, 3), "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f16x3 (f64 k-sums)" if prec == api.PREC_MIXED else "f64",
+            "data": "synthetic (seeded random tight-binding model)",
+            "config": {"workload": args.workload, "n_wf": model.n_wf, "n_R": model.n_R, "mesh": list(mp),
+                       "k_points_per_step": nk, "k_stride": ks, "valence_bands": job["valence_bands"], "n_eF": len(job["ef_lst"]),
+                       "form": args.precision, "l2": "flushed (256 MB write) before every step",
+                       "parallelism": f"replicas x{world}"},
+            "host_ms_per_step": 1e3 * t_host / args.steps,
+            "fp64_reruns_per_step": res["n_k_fp64"] if res else None,
+            "clocks": clk,
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                    "seconds_per_step": e2e_s},
+            "gpu_launches": launches,
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "error_vs_fp64": err,
+        }
+        print(json.dumps(out))
+
+
+def main():
+    args = parse()
+    rank, world = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_gpu(args, rank, world)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

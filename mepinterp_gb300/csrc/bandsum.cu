@@ -1,4 +1,5 @@
-// Band sums of one rank's k-points, accumulated over k in FP64:
+// Band sums of one rank's k-points; each k-point's tensors are formed in the
+// working precision T and accumulated over k in FP64:
 //   kubo_ahc_tens (src/kubo.f90:37-78)
 //       curv(i,j,n) = -2 sum_{m!=n} Im(V_i(n,m) V_j(m,n)) / (E_m - E_n)^2
 //       ahc(i,j,e) -= sum_n curv(i,j,n) f(e,n)
@@ -29,8 +30,8 @@ namespace {
 template <typename T>
 __device__ __forceinline__ T fd_stat(T e_band, double e_fermi, double T_kelvin) {  // src/statistics.f90:65-90
     if (T_kelvin > kMinTemp) {
-        double x = ((double)e_band - e_fermi) / (kKbEhK * T_kelvin);
-        return (T)(1.0 / (1.0 + exp(x)));
+        const T x = (e_band - (T)e_fermi) / (T)(kKbEhK * T_kelvin);
+        return (T)1 / ((T)1 + exp(x));
     }
     return ((double)e_band < e_fermi) ? (T)1 : (T)0;
 }
@@ -43,7 +44,8 @@ __device__ __forceinline__ void cross3(const cplx<T> a[3], const cplx<T> b[3], c
     out[2] = a[0] * b[1] - a[1] * b[0];
 }
 
-__device__ __forceinline__ double warp_sum(double v) {
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
@@ -57,17 +59,17 @@ __global__ void __launch_bounds__(256) bandsum_kernel(DevModel md, JobDev jb, in
     const int N = md.N, NN = N * N, ld = N + 1;
     const int nval = jb.nval, nE = jb.nE;
     cplx<T>* Vs = reinterpret_cast<cplx<T>*>(smem_raw);          // [3][N][ld]
-    double* curv = reinterpret_cast<double*>(Vs + 3 * N * ld);    // [9][N]
-    double* icn = curv + 9 * N;                                   // [9][N] Kubo IC per band
-    double* lcn = icn + 9 * N;                                    // [9][N] Kubo LC per band
-    double* icv = lcn + 9 * N;                                    // [9][kMaxN] Niu IC
-    double* lcv = icv + 9 * kMaxN;                                // [9][kMaxN] Niu LC
-    T* Es = reinterpret_cast<T*>(lcv + 9 * kMaxN);                // [N]
+    T* curv = reinterpret_cast<T*>(Vs + 3 * N * ld);              // [9][N]
+    T* icn = curv + 9 * N;                                        // [9][N] Kubo IC per band
+    T* lcn = icn + 9 * N;                                         // [9][N] Kubo LC per band
+    T* icv = lcn + 9 * N;                                         // [9][kMaxN] Niu IC
+    T* lcv = icv + 9 * kMaxN;                                     // [9][kMaxN] Niu LC
+    T* Es = lcv + 9 * kMaxN;                                      // [N]
     T* Cs = Es + kMaxN;                                           // [N]
     const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nwarps = nt >> 5;
     const AccLayout L{nE, nval};
     double* P = partials + (size_t)blockIdx.x * L.size();
-    const double tol = md.kubo_tol;
+    const T ttol = (T)md.kubo_tol;
 
     for (int64_t k = blockIdx.x; k < nk; k += gridDim.x) {
         if (skip && skip[k]) continue;
@@ -86,9 +88,9 @@ __global__ void __launch_bounds__(256) bandsum_kernel(DevModel md, JobDev jb, in
         for (int n0 = warp; n0 < N; n0 += nwarps) {
             const T E0 = Es[n0];
             const bool niu = (n0 < nval) && jb.do_mep;
-            double s_curv[9], s_ic[9], s_lc[9], s_icv[9], s_lcv[9];
+            T s_curv[9], s_ic[9], s_lc[9], s_icv[9], s_lcv[9];
 #pragma unroll
-            for (int q = 0; q < 9; ++q) s_curv[q] = s_ic[q] = s_lc[q] = s_icv[q] = s_lcv[q] = 0.0;
+            for (int q = 0; q < 9; ++q) s_curv[q] = s_ic[q] = s_lc[q] = s_icv[q] = s_lcv[q] = (T)0;
             cplx<T> vnn[3];
 #pragma unroll
             for (int c = 0; c < 3; ++c) vnn[c] = V(c, n0, n0);
@@ -105,7 +107,7 @@ __global__ void __launch_bounds__(256) bandsum_kernel(DevModel md, JobDev jb, in
 #pragma unroll
                     for (int j = 0; j < 3; ++j)
 #pragma unroll
-                        for (int i = 0; i < 3; ++i) s_curv[i + 3 * j] += -2.0 * (double)((vi[i] * vk[j]).im * inv);
+                        for (int i = 0; i < 3; ++i) s_curv[i + 3 * j] += (T)-2 * ((vi[i] * vk[j]).im * inv);
                 }
                 // LC
                 {
@@ -113,13 +115,13 @@ __global__ void __launch_bounds__(256) bandsum_kernel(DevModel md, JobDev jb, in
                     cross3(vk, vnn, x);
                     T den3 = d0n * d0n * d0n;
                     bool kubo_ok = jb.do_kubo;
-                    bool niu_ok = niu && (fabs((double)den3) > tol);
+                    bool niu_ok = niu && (fabs(den3) > ttol);
                     if (kubo_ok || niu_ok) {
 #pragma unroll
                         for (int j = 0; j < 3; ++j)
 #pragma unroll
                             for (int i = 0; i < 3; ++i) {
-                                double v = (double)((vi[i] * x[j]).re / den3);
+                                T v = (vi[i] * x[j]).re / den3;
                                 if (kubo_ok) s_lc[i + 3 * j] += v;
                                 if (niu_ok) s_lcv[i + 3 * j] += v;
                             }
@@ -141,7 +143,7 @@ __global__ void __launch_bounds__(256) bandsum_kernel(DevModel md, JobDev jb, in
                         const T b = (T)1 / d0m;
 #pragma unroll
                         for (int c = 0; c < 3; ++c) g[c] = g[c] + b * x[c];
-                        if (niu && fabs((double)(a2 * d0m)) > tol) {
+                        if (niu && fabs(a2 * d0m) > ttol) {
 #pragma unroll
                             for (int c = 0; c < 3; ++c) gv[c] = gv[c] + b * x[c];
                         }
@@ -151,15 +153,15 @@ __global__ void __launch_bounds__(256) bandsum_kernel(DevModel md, JobDev jb, in
                     for (int j = 0; j < 3; ++j)
 #pragma unroll
                         for (int i = 0; i < 3; ++i) {
-                            s_ic[i + 3 * j] += -(double)((vi[i] * g[j]).re * ainv);
-                            s_icv[i + 3 * j] += -(double)((vi[i] * gv[j]).re * ainv);
+                            s_ic[i + 3 * j] -= (vi[i] * g[j]).re * ainv;
+                            s_icv[i + 3 * j] -= (vi[i] * gv[j]).re * ainv;
                         }
                 }
             }
 #pragma unroll
             for (int q = 0; q < 9; ++q) {
-                double a = warp_sum(s_curv[q]), b = warp_sum(s_ic[q]), c = warp_sum(s_lc[q]);
-                double d = warp_sum(s_icv[q]), e = warp_sum(s_lcv[q]);
+                T a = warp_sum(s_curv[q]), b = warp_sum(s_ic[q]), c = warp_sum(s_lc[q]);
+                T d = warp_sum(s_icv[q]), e = warp_sum(s_lcv[q]);
                 if (lane == 0) {
                     curv[q * N + n0] = a;
                     icn[q * N + n0] = b;
@@ -173,8 +175,8 @@ __global__ void __launch_bounds__(256) bandsum_kernel(DevModel md, JobDev jb, in
         if (jb.do_mep) {
             for (int t = tid; t < 9 * nval; t += nt) {
                 int q = t % 9, n0 = t / 9;
-                P[L.mic_off() + q + 9 * n0] += icv[q * kMaxN + n0];
-                P[L.mlc_off() + q + 9 * n0] += lcv[q * kMaxN + n0];
+                P[L.mic_off() + q + 9 * n0] += (double)icv[q * kMaxN + n0];
+                P[L.mlc_off() + q + 9 * n0] += (double)lcv[q * kMaxN + n0];
                 if (q == 0 || q == 4 || q == 8) P[L.mcs_off() + q + 9 * n0] += (double)Cs[n0];
             }
         }
@@ -182,13 +184,13 @@ __global__ void __launch_bounds__(256) bandsum_kernel(DevModel md, JobDev jb, in
         if (nE >= 64) {
             for (int e = tid; e < nE; e += nt) {
                 const double ef = jb.ef[e];
-                double ne = 0, a[9], ki[9], kl[9], kc = 0;
+                T ne = 0, a[9], ki[9], kl[9], kc = 0;
 #pragma unroll
                 for (int q = 0; q < 9; ++q) a[q] = ki[q] = kl[q] = 0;
                 for (int n = 0; n < N; ++n) {
-                    double f = (double)fd_stat<T>(Es[n], ef, jb.T_kelvin);
+                    const T f = fd_stat<T>(Es[n], ef, jb.T_kelvin);
                     ne += f;
-                    kc += f * (double)Cs[n];
+                    kc += f * Cs[n];
 #pragma unroll
                     for (int q = 0; q < 9; ++q) {
                         a[q] -= curv[q * N + n] * f;
@@ -212,13 +214,13 @@ __global__ void __launch_bounds__(256) bandsum_kernel(DevModel md, JobDev jb, in
         } else {
             for (int e = warp; e < nE; e += nwarps) {
                 const double ef = jb.ef[e];
-                double ne = 0, a[9], ki[9], kl[9], kc = 0;
+                T ne = 0, a[9], ki[9], kl[9], kc = 0;
 #pragma unroll
                 for (int q = 0; q < 9; ++q) a[q] = ki[q] = kl[q] = 0;
                 for (int n = lane; n < N; n += 32) {
-                    double f = (double)fd_stat<T>(Es[n], ef, jb.T_kelvin);
+                    const T f = fd_stat<T>(Es[n], ef, jb.T_kelvin);
                     ne += f;
-                    kc += f * (double)Cs[n];
+                    kc += f * Cs[n];
 #pragma unroll
                     for (int q = 0; q < 9; ++q) {
                         a[q] -= curv[q * N + n] * f;
@@ -268,7 +270,7 @@ int bandsum_ctas() {
 template <typename T>
 size_t bandsum_smem(int N) {
     size_t b = 3 * (size_t)N * (N + 1) * sizeof(cplx<T>);
-    b += (27 * (size_t)N + 18 * kMaxN) * sizeof(double);
+    b += (27 * (size_t)N + 18 * kMaxN) * sizeof(T);
     b += 2 * kMaxN * sizeof(T);
     return (b + 15) & ~(size_t)15;
 }
