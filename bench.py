@@ -139,6 +139,8 @@ def flops_per_k(N, nR, nval, nE, has_r=True):
     r = 1 if has_r else 0
     return {
         "ft": 8.0 * nR * nb * N * N,
+        "fth": 8.0 * nR * N * N,
+        "refine": 3 * 8.0 * N ** 3,
         "eig": 80.0 / 3.0 * N ** 3,
         "rot": 16.0 * N ** 3 * (3 + 3 * r) + 24.0 * N ** 3 * r,
         "gauge": 180.0 * N * N,
@@ -236,7 +238,7 @@ def run_gpu(args, rank, world):
         res = ctx.core_worker_loc(job, precision=prec, k_stride=ks)
         t = ctx.timing()
         run_ms.append(t["run_ms"])
-        for key in ("ft", "phase", "eig", "rot", "gauge", "bandsum", "reduce"):
+        for key in api.STAGES:
             stage.setdefault(key, [0.0, 0])
             stage[key][0] += t[key + "_ms"]
             stage[key][1] += t[key + "_launches"]
@@ -267,7 +269,7 @@ def run_gpu(args, rank, world):
     # roofline of the dominant kernel (algorithmic flops / average launch time)
     f = flops_per_k(model.n_wf, model.n_R, job["valence_bands"], len(job["ef_lst"]), model.r is not None)
     stage_ms = {k: v[0] for k, v in stage.items()}
-    dom = max(("ft", "eig", "rot", "gauge", "bandsum"), key=lambda k: stage_ms.get(k, 0.0))
+    dom = max(("ft", "fth", "eig", "refine", "rot", "gauge", "bandsum"), key=lambda k: stage_ms.get(k, 0.0))
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))

@@ -120,11 +120,14 @@ typedef struct {
 typedef struct {
     double ft_ms;              /* Fourier sums (SIMT FP64 or tensor-core GEMM) */
     double phase_ms;           /* mixed form: phase-operand generation */
-    double eig_ms, rot_ms, gauge_ms, bandsum_ms, reduce_ms;
+    double fth_ms;             /* mixed form: FP64 Fourier sum of H(k) alone */
+    double eig_ms;             /* Jacobi eigensolver */
+    double refine_ms;          /* mixed form: FP64 eigenpair refinement */
+    double rot_ms, gauge_ms, bandsum_ms, reduce_ms;
     double total_ms;           /* sum of the stage times */
     double run_ms;             /* whole call, first launch to last copy back */
-    int32_t ft_launches, phase_launches, eig_launches, rot_launches, gauge_launches, bandsum_launches,
-        reduce_launches;
+    int32_t ft_launches, phase_launches, fth_launches, eig_launches, refine_launches, rot_launches,
+        gauge_launches, bandsum_launches, reduce_launches;
     int64_t n_k;               /* k-points of the run */
     int64_t h2d_bytes;         /* host->device bytes since mepi_create */
     int64_t d2h_bytes;         /* device->host bytes since mepi_create */

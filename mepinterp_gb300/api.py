@@ -62,14 +62,14 @@ class MepiAcc(C.Structure):
                 ("n_k_done", C.c_int64), ("n_k_fp64", C.c_int64), ("eig_max_sweeps", C.c_int32)]
 
 
+STAGES = ("ft", "phase", "fth", "eig", "refine", "rot", "gauge", "bandsum", "reduce")
+
+
 class MepiTiming(C.Structure):
-    _fields_ = [("ft_ms", C.c_double), ("phase_ms", C.c_double), ("eig_ms", C.c_double),
-                ("rot_ms", C.c_double), ("gauge_ms", C.c_double), ("bandsum_ms", C.c_double),
-                ("reduce_ms", C.c_double), ("total_ms", C.c_double), ("run_ms", C.c_double),
-                ("ft_launches", C.c_int32), ("phase_launches", C.c_int32), ("eig_launches", C.c_int32),
-                ("rot_launches", C.c_int32), ("gauge_launches", C.c_int32),
-                ("bandsum_launches", C.c_int32), ("reduce_launches", C.c_int32), ("n_k", C.c_int64),
-                ("h2d_bytes", C.c_int64), ("d2h_bytes", C.c_int64)]
+    _fields_ = ([(f"{s}_ms", C.c_double) for s in ("ft", "phase", "fth", "eig", "refine", "rot", "gauge",
+                                                   "bandsum", "reduce", "total", "run")]
+                + [(f"{s}_launches", C.c_int32) for s in STAGES]
+                + [("n_k", C.c_int64), ("h2d_bytes", C.c_int64), ("d2h_bytes", C.c_int64)])
 
 
 _lib: Optional[C.CDLL] = None

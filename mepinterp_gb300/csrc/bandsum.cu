@@ -28,12 +28,12 @@ namespace mepi {
 namespace {
 
 template <typename T>
-__device__ __forceinline__ T fd_stat(T e_band, double e_fermi, double T_kelvin) {  // src/statistics.f90:65-90
+__device__ __forceinline__ T fd_stat(double e_band, double e_fermi, double T_kelvin) {  // src/statistics.f90:65-90
     if (T_kelvin > kMinTemp) {
-        const T x = (e_band - (T)e_fermi) / (T)(kKbEhK * T_kelvin);
+        const T x = (T)((e_band - e_fermi) / (kKbEhK * T_kelvin));
         return (T)1 / ((T)1 + exp(x));
     }
-    return ((double)e_band < e_fermi) ? (T)1 : (T)0;
+    return (e_band < e_fermi) ? (T)1 : (T)0;
 }
 
 // cross(a, b)_j = sum_kl eps_jkl a_k b_l
@@ -52,7 +52,7 @@ __device__ __forceinline__ T warp_sum(T v) {
 }
 
 template <typename T>
-__global__ void __launch_bounds__(256) bandsum_kernel(DevModel md, JobDev jb, int64_t nk, const T* __restrict__ Eg,
+__global__ void __launch_bounds__(256) bandsum_kernel(DevModel md, JobDev jb, int64_t nk, const double* __restrict__ Eg,
                                                       const cplx<T>* __restrict__ Vg, const T* __restrict__ CSVg,
                                                       const int* __restrict__ skip, double* __restrict__ partials) {
     extern __shared__ unsigned char smem_raw[];
@@ -64,12 +64,12 @@ __global__ void __launch_bounds__(256) bandsum_kernel(DevModel md, JobDev jb, in
     T* lcn = icn + 9 * N;                                         // [9][N] Kubo LC per band
     T* icv = lcn + 9 * N;                                         // [9][kMaxN] Niu IC
     T* lcv = icv + 9 * kMaxN;                                     // [9][kMaxN] Niu LC
-    T* Es = lcv + 9 * kMaxN;                                      // [N]
-    T* Cs = Es + kMaxN;                                           // [N]
+    T* Cs = lcv + 9 * kMaxN;                                      // [kMaxN]
+    double* Es = reinterpret_cast<double*>(Cs + kMaxN);           // [kMaxN], 8-byte aligned below
     const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nwarps = nt >> 5;
     const AccLayout L{nE, nval};
     double* P = partials + (size_t)blockIdx.x * L.size();
-    const T ttol = (T)md.kubo_tol;
+    const double tol = md.kubo_tol;
 
     for (int64_t k = blockIdx.x; k < nk; k += gridDim.x) {
         if (skip && skip[k]) continue;
@@ -86,7 +86,7 @@ __global__ void __launch_bounds__(256) bandsum_kernel(DevModel md, JobDev jb, in
         auto V = [&](int a, int n, int m) -> cplx<T> { return Vs[(a * N + n) * ld + m]; };
 
         for (int n0 = warp; n0 < N; n0 += nwarps) {
-            const T E0 = Es[n0];
+            const double E0 = Es[n0];
             const bool niu = (n0 < nval) && jb.do_mep;
             T s_curv[9], s_ic[9], s_lc[9], s_icv[9], s_lcv[9];
 #pragma unroll
@@ -96,8 +96,8 @@ __global__ void __launch_bounds__(256) bandsum_kernel(DevModel md, JobDev jb, in
             for (int c = 0; c < 3; ++c) vnn[c] = V(c, n0, n0);
             for (int n = lane; n < N; n += 32) {
                 if (n == n0) continue;
-                const T En = Es[n];
-                const T d0n = E0 - En;  // E0 - En
+                const double d0nd = E0 - Es[n];  // E0 - En in FP64
+                const T d0n = (T)d0nd;
                 cplx<T> vi[3], vk[3];
 #pragma unroll
                 for (int c = 0; c < 3; ++c) { vi[c] = V(c, n0, n); vk[c] = V(c, n, n0); }
@@ -113,9 +113,9 @@ __global__ void __launch_bounds__(256) bandsum_kernel(DevModel md, JobDev jb, in
                 {
                     cplx<T> x[3];
                     cross3(vk, vnn, x);
-                    T den3 = d0n * d0n * d0n;
+                    const T den3 = d0n * d0n * d0n;
                     bool kubo_ok = jb.do_kubo;
-                    bool niu_ok = niu && (fabs(den3) > ttol);
+                    bool niu_ok = niu && (fabs(d0nd * d0nd * d0nd) > tol);
                     if (kubo_ok || niu_ok) {
 #pragma unroll
                         for (int j = 0; j < 3; ++j)
@@ -133,17 +133,18 @@ __global__ void __launch_bounds__(256) bandsum_kernel(DevModel md, JobDev jb, in
 #pragma unroll
                     for (int c = 0; c < 3; ++c) g[c] = gv[c] = mk((T)0, (T)0);
                     const T a2 = d0n * d0n;
+                    const double a2d = d0nd * d0nd;
                     for (int m = 0; m < N; ++m) {
                         if (m == n0) continue;
                         cplx<T> vnm[3], vmo[3], x[3];
 #pragma unroll
                         for (int c = 0; c < 3; ++c) { vnm[c] = V(c, n, m); vmo[c] = V(c, m, n0); }
                         cross3(vnm, vmo, x);
-                        const T d0m = E0 - Es[m];
-                        const T b = (T)1 / d0m;
+                        const double d0md = E0 - Es[m];
+                        const T b = (T)(1.0 / d0md);
 #pragma unroll
                         for (int c = 0; c < 3; ++c) g[c] = g[c] + b * x[c];
-                        if (niu && fabs(a2 * d0m) > ttol) {
+                        if (niu && fabs(a2d * d0md) > tol) {
 #pragma unroll
                             for (int c = 0; c < 3; ++c) gv[c] = gv[c] + b * x[c];
                         }
@@ -270,13 +271,14 @@ int bandsum_ctas() {
 template <typename T>
 size_t bandsum_smem(int N) {
     size_t b = 3 * (size_t)N * (N + 1) * sizeof(cplx<T>);
-    b += (27 * (size_t)N + 18 * kMaxN) * sizeof(T);
-    b += 2 * kMaxN * sizeof(T);
+    b += (27 * (size_t)N + 18 * kMaxN + kMaxN) * sizeof(T);
+    b = (b + 7) & ~(size_t)7;
+    b += kMaxN * sizeof(double);
     return (b + 15) & ~(size_t)15;
 }
 
 template <typename T>
-cudaError_t launch_bandsum(const DevModel& m, const JobDev& j, int64_t nk, const T* E, const cplx<T>* V, const T* CSV,
+cudaError_t launch_bandsum(const DevModel& m, const JobDev& j, int64_t nk, const double* E, const cplx<T>* V, const T* CSV,
                            const int* skip, double* partials, int n_cta, cudaStream_t s) {
     if (nk <= 0) return cudaSuccess;
     size_t smem = bandsum_smem<T>(m.N);
@@ -293,7 +295,7 @@ cudaError_t launch_reduce(const double* partials, int n_cta, int size, double* o
 
 template cudaError_t launch_bandsum<double>(const DevModel&, const JobDev&, int64_t, const double*,
                                             const cplx<double>*, const double*, const int*, double*, int, cudaStream_t);
-template cudaError_t launch_bandsum<float>(const DevModel&, const JobDev&, int64_t, const float*, const cplx<float>*,
+template cudaError_t launch_bandsum<float>(const DevModel&, const JobDev&, int64_t, const double*, const cplx<float>*,
                                            const float*, const int*, double*, int, cudaStream_t);
 
 }  // namespace mepi

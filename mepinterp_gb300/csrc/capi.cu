@@ -53,7 +53,7 @@ struct StageEv {
     int stage;
 };
 
-enum { ST_FT = 0, ST_PHASE, ST_EIG, ST_ROT, ST_GAUGE, ST_BAND, ST_RED, ST_RUN, ST_N };
+enum { ST_FT = 0, ST_PHASE, ST_FTH, ST_EIG, ST_REFINE, ST_ROT, ST_GAUGE, ST_BAND, ST_RED, ST_RUN, ST_N };
 
 }  // namespace
 
@@ -65,7 +65,7 @@ struct mepi_ctx {
     double a_latt[9];
     DevBuf S, R, tau;
     // per-chunk work buffers
-    DevBuf W, E, U, HA, OD, V, CSV, ODH, flags, klist, kpts, partials, out, counters;
+    DevBuf W, E, E64, H64, U, HA, OD, V, CSV, ODH, flags, klist, kpts, partials, out, counters;
     int* h_flags = nullptr;  // pinned
     size_t h_flags_cap = 0;
     std::vector<StageEv> events;
@@ -75,6 +75,7 @@ struct mepi_ctx {
     std::vector<cplx<double>> S_host;  // FP64 stack, kept to build the tensor-core operands
     TcPlan tc;
     bool ft_simt_only = false;          // MEPI_FT_SIMT=1: FP64 SIMT Fourier sums in the mixed form too
+    int first_order = 1;                // MEPI_REFINE_FIRST_ORDER=0: energies-only refinement
 };
 
 namespace {
@@ -129,7 +130,7 @@ template <typename T>
 size_t per_k_bytes(int N, int nb) {
     size_t NN = (size_t)N * N;
     return sizeof(cplx<T>) * (nb * NN + NN + 6 * NN + 3 * N + 3 * NN + 3 * N) + sizeof(T) * 2 * N + sizeof(int) +
-           sizeof(int64_t);
+           sizeof(int64_t) + sizeof(double) * N + (sizeof(T) == 4 ? sizeof(cplx<double>) * NN : 0);
 }
 
 template <typename T>
@@ -137,6 +138,8 @@ int ensure_chunk(mepi_ctx* ctx, int64_t chunk) {
     const size_t NN = (size_t)ctx->N * ctx->N, N = ctx->N;
     CKM(ctx->W.ensure(chunk * ctx->nb * NN * sizeof(cplx<T>)));
     CKM(ctx->E.ensure(chunk * N * sizeof(T)));
+    CKM(ctx->E64.ensure(chunk * N * sizeof(double)));
+    if (sizeof(T) == 4) CKM(ctx->H64.ensure(chunk * NN * sizeof(cplx<double>)));
     CKM(ctx->U.ensure(chunk * NN * sizeof(cplx<T>)));
     CKM(ctx->HA.ensure(chunk * 6 * NN * sizeof(cplx<T>)));
     CKM(ctx->OD.ensure(chunk * 3 * N * sizeof(cplx<T>)));
@@ -146,13 +149,18 @@ int ensure_chunk(mepi_ctx* ctx, int64_t chunk) {
     return 0;
 }
 
-// One chunk of k-points through FT -> eig -> rot -> gauge (-> bandsum).
+// One chunk of k-points through FT -> eig (-> FP64 refinement) -> rot ->
+// gauge (-> bandsum).  The band kernels always consume FP64 energies: the
+// FP64 path's Jacobi writes them directly; the mixed path refines the FP32
+// eigenpairs against an FP64 H(k) first.
 template <typename T>
 int run_chunk(mepi_ctx* ctx, const KRange& kr, const JobDev* jb, int n_cta, double degen_gap, bool want_flags,
               bool bandsum, cplx<T>* odh) {
     const int64_t nk = kr.count;
     int* counters = ctx->counters.as<int>();
-    if (sizeof(T) == 4 && !ctx->ft_simt_only) {
+    const bool mixed = sizeof(T) == 4;
+    int* flags = want_flags ? ctx->flags.as<int>() : nullptr;
+    if (mixed && !ctx->ft_simt_only) {
         if (!ctx->tc.ready()) {
             int rc = tc_plan_init(ctx->tc, ctx->dm, ctx->S_host.data());
             if (rc) return rc;
@@ -165,17 +173,25 @@ int run_chunk(mepi_ctx* ctx, const KRange& kr, const JobDev* jb, int n_cta, doub
     } else {
         STAGE(ST_FT, (launch_ft_simt<T>(ctx->dm, kr, ctx->W.as<cplx<T>>(), ctx->stream)));
     }
-    STAGE(ST_EIG, (launch_eig<T>(ctx->N, nk, ctx->W.as<cplx<T>>(), ctx->nb, ctx->E.as<T>(), ctx->U.as<cplx<T>>(), 40,
-                                 counters, counters + (sizeof(T) == 8 ? 1 : 2), degen_gap, want_flags ? ctx->flags.as<int>() : nullptr,
-                                 ctx->stream)));
+    double* E64 = ctx->E64.as<double>();
+    if (mixed) {
+        cplx<double>* H64 = ctx->H64.as<cplx<double>>();
+        STAGE(ST_FTH, launch_ft_h64(ctx->dm, kr, H64, ctx->stream));
+        STAGE(ST_EIG, (launch_eig<T>(ctx->N, nk, ctx->W.as<cplx<T>>(), ctx->nb, H64, ctx->E.as<T>(),
+                                     ctx->U.as<cplx<T>>(), 40, counters, counters + 2, degen_gap, flags, ctx->stream)));
+        STAGE(ST_REFINE, launch_refine(ctx->N, nk, H64, reinterpret_cast<cplx<float>*>(ctx->U.p), E64, degen_gap,
+                                       ctx->first_order, flags, ctx->stream));
+    } else {
+        STAGE(ST_EIG, (launch_eig<T>(ctx->N, nk, ctx->W.as<cplx<T>>(), ctx->nb, nullptr, reinterpret_cast<T*>(E64),
+                                     ctx->U.as<cplx<T>>(), 40, counters, counters + 1, degen_gap, flags, ctx->stream)));
+    }
     STAGE(ST_ROT, (launch_rot<T>(ctx->dm, nk, ctx->W.as<cplx<T>>(), ctx->U.as<cplx<T>>(), ctx->HA.as<cplx<T>>(),
                                  ctx->OD.as<cplx<T>>(), ctx->stream)));
-    STAGE(ST_GAUGE, (launch_gauge<T>(ctx->dm, nk, ctx->E.as<T>(), ctx->HA.as<cplx<T>>(), ctx->OD.as<cplx<T>>(),
+    STAGE(ST_GAUGE, (launch_gauge<T>(ctx->dm, nk, E64, ctx->HA.as<cplx<T>>(), ctx->OD.as<cplx<T>>(),
                                      ctx->V.as<cplx<T>>(), ctx->CSV.as<T>(), odh, ctx->stream)));
     if (bandsum)
-        STAGE(ST_BAND, (launch_bandsum<T>(ctx->dm, *jb, nk, ctx->E.as<T>(), ctx->V.as<cplx<T>>(), ctx->CSV.as<T>(),
-                                          want_flags ? ctx->flags.as<int>() : nullptr, ctx->partials.as<double>(),
-                                          n_cta, ctx->stream)));
+        STAGE(ST_BAND, (launch_bandsum<T>(ctx->dm, *jb, nk, E64, ctx->V.as<cplx<T>>(), ctx->CSV.as<T>(), flags,
+                                          ctx->partials.as<double>(), n_cta, ctx->stream)));
     return 0;
 }
 
@@ -188,7 +204,9 @@ int collect_timing(mepi_ctx* ctx, int64_t nk) {
         switch (ctx->events[i].stage) {
             case ST_FT: t.ft_ms += ms; t.ft_launches++; break;
             case ST_PHASE: t.phase_ms += ms; t.phase_launches++; break;
+            case ST_FTH: t.fth_ms += ms; t.fth_launches++; break;
             case ST_EIG: t.eig_ms += ms; t.eig_launches++; break;
+            case ST_REFINE: t.refine_ms += ms; t.refine_launches++; break;
             case ST_ROT: t.rot_ms += ms; t.rot_launches++; break;
             case ST_GAUGE: t.gauge_ms += ms; t.gauge_launches++; break;
             case ST_BAND: t.bandsum_ms += ms; t.bandsum_launches++; break;
@@ -197,7 +215,8 @@ int collect_timing(mepi_ctx* ctx, int64_t nk) {
             default: break;
         }
     }
-    t.total_ms = t.ft_ms + t.phase_ms + t.eig_ms + t.rot_ms + t.gauge_ms + t.bandsum_ms + t.reduce_ms;
+    t.total_ms = t.ft_ms + t.phase_ms + t.fth_ms + t.eig_ms + t.refine_ms + t.rot_ms + t.gauge_ms + t.bandsum_ms +
+                 t.reduce_ms;
     t.h2d_bytes = ctx->h2d;
     t.d2h_bytes = ctx->d2h;
     ctx->timing = t;
@@ -441,6 +460,8 @@ int mepi_create(mepi_ctx** out, const mepi_model* m) {
     }
     const char* simt_env = std::getenv("MEPI_FT_SIMT");
     ctx->ft_simt_only = simt_env && simt_env[0] == '1';
+    const char* fo_env = std::getenv("MEPI_REFINE_FIRST_ORDER");
+    ctx->first_order = (fo_env && fo_env[0] == '0') ? 0 : 1;
     std::vector<double> Rh(3 * (size_t)nR);
     std::memcpy(Rh.data(), m->R_frac, Rh.size() * sizeof(double));
     if (ctx->S.ensure(S.size() * sizeof(cplx<double>)) != cudaSuccess) return fail(MEPI_ERR_NOMEM);
@@ -517,9 +538,9 @@ int mepi_interp_k(mepi_ctx* ctx, int32_t precision, int64_t n_k, const double* k
                 rc = run_chunk<float>(ctx, kr, nullptr, 0, 0.0, false, false, ctx->ODH.as<cplx<float>>());
             if (rc) return rc;
             // copy back and convert to double
-            std::vector<unsigned char> bE(cn * N * esz), bV(cn * 3 * NN * 2 * esz), bHA(cn * 6 * NN * 2 * esz),
-                bO(cn * 3 * N * 2 * esz);
-            CK(cudaMemcpyAsync(bE.data(), ctx->E.p, bE.size(), cudaMemcpyDeviceToHost, ctx->stream));
+            std::vector<unsigned char> bV(cn * 3 * NN * 2 * esz), bHA(cn * 6 * NN * 2 * esz), bO(cn * 3 * N * 2 * esz);
+            std::vector<double> bE(cn * N);
+            CK(cudaMemcpyAsync(bE.data(), ctx->E64.p, bE.size() * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
             CK(cudaMemcpyAsync(bV.data(), ctx->V.p, bV.size(), cudaMemcpyDeviceToHost, ctx->stream));
             CK(cudaMemcpyAsync(bHA.data(), ctx->HA.p, bHA.size(), cudaMemcpyDeviceToHost, ctx->stream));
             CK(cudaMemcpyAsync(bO.data(), ctx->ODH.p, bO.size(), cudaMemcpyDeviceToHost, ctx->stream));
@@ -534,7 +555,7 @@ int mepi_interp_k(mepi_ctx* ctx, int32_t precision, int64_t n_k, const double* k
                     for (size_t i = 0; i < n; ++i) dst[off + i] = f[i];
                 }
             };
-            conv(bE, hE);
+            hE.insert(hE.end(), bE.begin(), bE.end());
             conv(bV, hV);
             conv(bHA, hHA);
             conv(bO, hO);
@@ -606,7 +627,8 @@ int mepi_destroy(mepi_ctx* ctx) {
     if (!ctx) return MEPI_OK;
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
-    for (DevBuf* b : {&ctx->S, &ctx->R, &ctx->tau, &ctx->W, &ctx->E, &ctx->U, &ctx->HA, &ctx->OD, &ctx->V, &ctx->CSV,
+    for (DevBuf* b : {&ctx->S, &ctx->R, &ctx->tau, &ctx->W, &ctx->E, &ctx->E64, &ctx->H64, &ctx->U, &ctx->HA,
+                      &ctx->OD, &ctx->V, &ctx->CSV,
                       &ctx->ODH, &ctx->flags, &ctx->klist, &ctx->kpts, &ctx->partials, &ctx->out, &ctx->counters})
         b->release();
     for (auto& ev : ctx->events) {

@@ -30,6 +30,7 @@ template <> struct EigTol<float> { static constexpr double eps = 1.1920928955078
 
 template <typename T>
 __global__ void __launch_bounds__(256) jacobi_kernel(int N, const cplx<T>* __restrict__ W, int nbW,
+                                                     const cplx<double>* __restrict__ H64,
                                                      T* __restrict__ E, cplx<T>* __restrict__ U, int max_sweeps,
                                                      int* sweeps_max, int* flag_cap, double degen_gap,
                                                      int* redo_flag) {
@@ -48,15 +49,19 @@ __global__ void __launch_bounds__(256) jacobi_kernel(int N, const cplx<T>* __res
 
     const int tid = threadIdx.x, nt = blockDim.x;
     const int64_t k = blockIdx.x;
-    const cplx<T>* Hk = W + (size_t)k * nbW * N * N;
     const int NN = N * N;
-    // load, Hermitise from the upper triangle
+    // load (from the FP64 H(k) when given), Hermitise from the upper triangle
     for (int e = tid; e < NN; e += nt) {
         int i = e / N, j = e % N;
-        cplx<T> v;
-        if (i < j) v = Hk[i * N + j];
-        else if (i > j) v = conjg(Hk[j * N + i]);
-        else v = mk(Hk[i * N + i].re, (T)0);
+        int a = i < j ? i : j, b = i < j ? j : i;
+        cplx<T> h;
+        if (H64) {
+            const cplx<double> x = H64[(size_t)k * NN + a * N + b];
+            h = mk((T)x.re, (T)x.im);
+        } else {
+            h = W[(size_t)k * nbW * NN + a * N + b];
+        }
+        cplx<T> v = (i < j) ? h : (i > j) ? conjg(h) : mk(h.re, (T)0);
         M[i * ld + j] = v;
         Vv[i * ld + j] = mk((T)(i == j ? 1 : 0), (T)0);
     }
@@ -115,9 +120,10 @@ __global__ void __launch_bounds__(256) jacobi_kernel(int N, const cplx<T>* __res
                 pp[tid] = p; qq[tid] = q; cs[tid] = c; ss[tid] = s; eph[tid] = ph;
             }
             __syncthreads();
-            // 2. column pass M <- M G and U <- U G
+            // 2. column pass M <- M G and U <- U G (consecutive threads walk the
+            //    rows of one pair: padded rows put them in distinct banks)
             for (int e = tid; e < N * half; e += nt) {
-                int i = e / half, j = e % half;
+                int j = e / N, i = e % N;
                 int p = pp[j], q = qq[j];
                 if (p < 0) continue;
                 T c = cs[j], s = ss[j];
@@ -131,9 +137,9 @@ __global__ void __launch_bounds__(256) jacobi_kernel(int N, const cplx<T>* __res
                 Vv[i * ld + q] = s * (ph * vp) + c * vq;
             }
             __syncthreads();
-            // 3. row pass M <- G^dag M
+            // 3. row pass M <- G^dag M (consecutive threads walk one row)
             for (int e = tid; e < N * half; e += nt) {
-                int i = e / half, j = e % half;
+                int j = e / N, i = e % N;
                 int p = pp[j], q = qq[j];
                 if (p < 0) continue;
                 T c = cs[j], s = ss[j];
@@ -218,21 +224,117 @@ size_t eig_smem_bytes(int N) {
 }
 
 template <typename T>
-cudaError_t launch_eig(int N, int64_t nk, const cplx<T>* W, int nbW, T* E, cplx<T>* U, int max_sweeps,
-                       int* sweeps_max, int* flag_cap, double degen_gap, int* redo_flag, cudaStream_t s) {
+cudaError_t launch_eig(int N, int64_t nk, const cplx<T>* W, int nbW, const cplx<double>* H64, T* E, cplx<T>* U,
+                       int max_sweeps, int* sweeps_max, int* flag_cap, double degen_gap, int* redo_flag,
+                       cudaStream_t s) {
     if (nk <= 0) return cudaSuccess;
     size_t smem = eig_smem_bytes<T>(N);
     cudaError_t e = cudaFuncSetAttribute(jacobi_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     int threads = N <= 16 ? 128 : 256;
-    jacobi_kernel<T><<<(unsigned)nk, threads, smem, s>>>(N, W, nbW, E, U, max_sweeps, sweeps_max, flag_cap, degen_gap,
-                                                         redo_flag);
+    jacobi_kernel<T><<<(unsigned)nk, threads, smem, s>>>(N, W, nbW, H64, E, U, max_sweeps, sweeps_max, flag_cap,
+                                                         degen_gap, redo_flag);
     return cudaGetLastError();
 }
 
-template cudaError_t launch_eig<double>(int, int64_t, const cplx<double>*, int, double*, cplx<double>*, int, int*, int*,
-                                        double, int*, cudaStream_t);
-template cudaError_t launch_eig<float>(int, int64_t, const cplx<float>*, int, float*, cplx<float>*, int, int*, int*,
-                                       double, int*, cudaStream_t);
+// FP64 refinement of FP32 eigenpairs against the FP64 H(k):
+//   T = H U, H' = U^dag T (both FP64), E_n = Re H'_nn (Rayleigh quotients, whose
+//   error is second order in the FP32 eigenvector error), and, when first_order
+//   is set, U <- U (1 + X) with X_mn = H'_mn / (E_n - E_m) for the pairs whose
+//   gap exceeds degen_gap.  A k-point with a gap at or below degen_gap, or with
+//   non-finite values, is flagged for the full FP64 rerun.  Eigenpairs are
+//   re-sorted by the refined energies.
+__global__ void __launch_bounds__(256) refine_kernel(int N, const cplx<double>* __restrict__ H64,
+                                                     cplx<float>* __restrict__ U, double* __restrict__ E64,
+                                                     double degen_gap, int first_order, int* __restrict__ redo_flag) {
+    extern __shared__ unsigned char smem_raw[];
+    const int NN = N * N;
+    cplx<double>* Hs = reinterpret_cast<cplx<double>*>(smem_raw);
+    cplx<double>* Us = Hs + NN;
+    cplx<double>* Ts = Us + NN;
+    double* Ev = reinterpret_cast<double*>(Ts + NN);
+    __shared__ int s_flag;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const int64_t k = blockIdx.x;
+    for (int e = tid; e < NN; e += nt) {
+        int i = e / N, j = e % N;
+        int a = i < j ? i : j, b = i < j ? j : i;
+        cplx<double> h = H64[(size_t)k * NN + a * N + b];
+        Hs[e] = (i < j) ? h : (i > j) ? conjg(h) : mk(h.re, 0.0);
+        const cplx<float> u = U[(size_t)k * NN + e];
+        Us[e] = mk((double)u.re, (double)u.im);
+    }
+    if (tid == 0) s_flag = redo_flag ? redo_flag[k] : 0;
+    __syncthreads();
+    // T = H U
+    for (int e = tid; e < NN; e += nt) {
+        int i = e / N, c = e % N;
+        cplx<double> acc = mk(0.0, 0.0);
+        for (int l = 0; l < N; ++l) fma_c(acc, Hs[i * N + l], Us[l * N + c]);
+        Ts[e] = acc;
+    }
+    __syncthreads();
+    // H' = U^dag T  (into Hs)
+    for (int e = tid; e < NN; e += nt) {
+        int i = e / N, c = e % N;
+        cplx<double> acc = mk(0.0, 0.0);
+        for (int l = 0; l < N; ++l) fma_cjc(acc, Us[l * N + i], Ts[l * N + c]);
+        Hs[e] = acc;
+    }
+    __syncthreads();
+    for (int n = tid; n < N; n += nt) Ev[n] = Hs[n * N + n].re;
+    __syncthreads();
+    // flag near degeneracies (and non-finite energies)
+    for (int e = tid; e < NN; e += nt) {
+        int i = e / N, j = e % N;
+        if (i < j && !(fabs(Ev[i] - Ev[j]) > degen_gap)) s_flag = 1;
+    }
+    if (first_order) {
+        // X into Ts, then U' = U + U X into Hs
+        for (int e = tid; e < NN; e += nt) {
+            int m = e / N, n = e % N;
+            const double d = Ev[n] - Ev[m];
+            Ts[e] = (m != n && fabs(d) > degen_gap) ? mk(Hs[e].re / d, Hs[e].im / d) : mk(0.0, 0.0);
+        }
+        __syncthreads();
+        for (int e = tid; e < NN; e += nt) {
+            int i = e / N, n = e % N;
+            cplx<double> acc = Us[e];
+            for (int m = 0; m < N; ++m) fma_c(acc, Us[i * N + m], Ts[m * N + n]);
+            Hs[e] = acc;
+        }
+        __syncthreads();
+        for (int e = tid; e < NN; e += nt) Us[e] = Hs[e];
+    }
+    __syncthreads();
+    for (int n = tid; n < N; n += nt) {
+        const double en = Ev[n];
+        int rank = 0;
+        for (int j = 0; j < N; ++j) rank += (Ev[j] < en || (Ev[j] == en && j < n)) ? 1 : 0;
+        E64[(size_t)k * N + rank] = en;
+        for (int row = 0; row < N; ++row) {
+            const cplx<double> u = Us[row * N + n];
+            U[(size_t)k * NN + row * N + rank] = mk((float)u.re, (float)u.im);
+        }
+        if (!isfinite(en)) s_flag = 1;
+    }
+    __syncthreads();
+    if (tid == 0 && redo_flag) redo_flag[k] = s_flag ? 1 : 0;
+}
+
+cudaError_t launch_refine(int N, int64_t nk, const cplx<double>* H64, cplx<float>* U, double* E64, double degen_gap,
+                          int first_order, int* redo_flag, cudaStream_t s) {
+    if (nk <= 0) return cudaSuccess;
+    const size_t smem = 3 * (size_t)N * N * sizeof(cplx<double>) + (size_t)N * sizeof(double);
+    cudaError_t e = cudaFuncSetAttribute(refine_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    refine_kernel<<<(unsigned)nk, N <= 16 ? 128 : 256, smem, s>>>(N, H64, U, E64, degen_gap, first_order, redo_flag);
+    return cudaGetLastError();
+}
+
+template cudaError_t launch_eig<double>(int, int64_t, const cplx<double>*, int, const cplx<double>*, double*,
+                                        cplx<double>*, int, int*, int*, double, int*, cudaStream_t);
+template cudaError_t launch_eig<float>(int, int64_t, const cplx<float>*, int, const cplx<double>*, float*,
+                                       cplx<float>*, int, int*, int*, double, int*, cudaStream_t);
 
 }  // namespace mepi

@@ -133,7 +133,90 @@ __global__ void __launch_bounds__(NT) ft_simt_kernel(DevModel m, KRange kr, cplx
         }
     }
 }
+// H(k) alone in FP64 for the mixed form's energy refinement: the same
+// contraction restricted to stack block 0 (read with the stack's block stride),
+// 8 k-points x 1 pair per thread, tau phase applied, H64[k][n][m] written.
+constexpr int HK = 64, HP = 32;
+__global__ void __launch_bounds__(NT) ft_h64_kernel(DevModel m, KRange kr, cplx<double>* __restrict__ H64) {
+    __shared__ cplx<double> Ps[RT][HK];
+    __shared__ cplx<double> Ss[RT][HP];
+    __shared__ double ks[HK][3];
+    const int tid = threadIdx.x;
+    const int NN = m.N * m.N;
+    const int64_t k0 = (int64_t)blockIdx.x * HK;
+    const int p0 = blockIdx.y * HP;
+    const int pl = tid % HP, kg = tid / HP;  // kg 0..7 -> k = kg + 8 j
+    if (tid < HK) {
+        double k[3] = {0.0, 0.0, 0.0};
+        int64_t i = k0 + tid;
+        if (i < kr.count) {
+            if (kr.kpts) {
+                k[0] = kr.kpts[3 * i]; k[1] = kr.kpts[3 * i + 1]; k[2] = kr.kpts[3 * i + 2];
+            } else {
+                mp_kpt(kr.mp, k_of(kr, i), k);
+            }
+        }
+        ks[tid][0] = k[0]; ks[tid][1] = k[1]; ks[tid][2] = k[2];
+    }
+    cplx<double> acc[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) acc[j] = mk(0.0, 0.0);
+    for (int r0 = 0; r0 < m.nR; r0 += RT) {
+        __syncthreads();
+        for (int e = tid; e < HK * RT; e += NT) {
+            int rr = e / HK, kk = e % HK, R = r0 + rr;
+            cplx<double> v = mk(0.0, 0.0);
+            if (R < m.nR) {
+                double x = ks[kk][0] * m.R[3 * R] + ks[kk][1] * m.R[3 * R + 1] + ks[kk][2] * m.R[3 * R + 2];
+                double sn, cs;
+                sincospi(2.0 * x, &sn, &cs);
+                v = mk(cs, sn);
+            }
+            Ps[rr][kk] = v;
+        }
+        for (int e = tid; e < RT * HP; e += NT) {
+            int rr = e / HP, q = e % HP, R = r0 + rr, pair = p0 + q;
+            cplx<double> v = mk(0.0, 0.0);
+            if (R < m.nR && pair < NN) v = m.S[((size_t)R * NN + pair) * m.nb];
+            Ss[rr][q] = v;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int rr = 0; rr < RT; ++rr) {
+            const cplx<double> s = Ss[rr][pl];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) fma_c(acc[j], Ps[rr][kg + 8 * j], s);
+        }
+    }
+    const int pair = p0 + pl;
+    if (pair >= NN) return;
+    const int n = pair / m.N, mm = pair % m.N;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        const int kk = kg + 8 * j;
+        const int64_t i = k0 + kk;
+        if (i >= kr.count) continue;
+        cplx<double> psi = mk(1.0, 0.0);
+        if (m.has_tau) {
+            double x = 0.0;
+            for (int c = 0; c < 3; ++c) x += ks[kk][c] * (m.tau[mm * 3 + c] - m.tau[n * 3 + c]);
+            double sn, cs;
+            sincospi(2.0 * x, &sn, &cs);
+            psi = mk(cs, sn);
+        }
+        H64[(size_t)i * NN + pair] = psi * acc[j];
+    }
+}
+
 }  // namespace
+
+cudaError_t launch_ft_h64(const DevModel& m, const KRange& kr, cplx<double>* H64, cudaStream_t s) {
+    if (kr.count <= 0) return cudaSuccess;
+    const int NN = m.N * m.N;
+    dim3 grid((unsigned)((kr.count + HK - 1) / HK), (unsigned)((NN + HP - 1) / HP));
+    ft_h64_kernel<<<grid, NT, 0, s>>>(m, kr, H64);
+    return cudaGetLastError();
+}
 
 template <typename T>
 cudaError_t launch_ft_simt(const DevModel& m, const KRange& kr, cplx<T>* W, cudaStream_t s) {

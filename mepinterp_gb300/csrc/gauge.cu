@@ -23,15 +23,12 @@ namespace {
 template <typename T>
 struct GaugeCtx {
     const cplx<T>* HA;  // [6][N][N] of this k
-    const T* E;
-    int N, do_gauge, semantics;
-    T tol;
+    const T* invd;      // [N][N] 1/(E_m - E_n) where D is defined, else 0 (shared memory)
+    int N, semantics;
     __device__ __forceinline__ cplx<T> D(int a, int n, int m) const {
-        if (!do_gauge || n == m) return mk((T)0, (T)0);
-        T de = E[m] - E[n];
-        if (!(fabs(de) > tol)) return mk((T)0, (T)0);
-        cplx<T> h = HA[(size_t)a * N * N + n * N + m];
-        return mk(h.re / de, h.im / de);
+        const T w = invd[n * N + m];
+        const cplx<T> h = HA[(size_t)a * N * N + n * N + m];
+        return mk(h.re * w, h.im * w);
     }
     // A' used in the curvature commutators
     __device__ __forceinline__ cplx<T> Ac(int a, int n, int m) const {
@@ -42,23 +39,30 @@ struct GaugeCtx {
 };
 
 template <typename T>
-__global__ void __launch_bounds__(256) gauge_kernel(DevModel m, const T* __restrict__ Eg, const cplx<T>* __restrict__ HA,
+__global__ void __launch_bounds__(256) gauge_kernel(DevModel m, const double* __restrict__ Eg, const cplx<T>* __restrict__ HA,
                                                     const cplx<T>* __restrict__ OD, cplx<T>* __restrict__ V,
                                                     T* __restrict__ CSV, cplx<T>* __restrict__ ODH) {
     const int N = m.N, NN = N * N;
     const int tid = threadIdx.x, nt = blockDim.x;
     const int64_t k = blockIdx.x;
-    __shared__ T Es[kMaxN];
+    __shared__ double Es[kMaxN];
     __shared__ cplx<T> Oh[3][kMaxN];
+    extern __shared__ unsigned char smem_raw[];
+    T* invd = reinterpret_cast<T*>(smem_raw);
     for (int n = tid; n < N; n += nt) Es[n] = Eg[(size_t)k * N + n];
+    __syncthreads();
+    // inverse gaps of the covariant derivative, decided and formed in FP64
+    for (int e = tid; e < NN; e += nt) {
+        const int n = e / N, mm = e % N;
+        const double ded = Es[mm] - Es[n];
+        invd[e] = (m.do_gauge && n != mm && fabs(ded) > m.kubo_tol) ? (T)(1.0 / ded) : (T)0;
+    }
     __syncthreads();
     GaugeCtx<T> g;
     g.HA = HA + (size_t)k * 6 * NN;
-    g.E = Es;
+    g.invd = invd;
     g.N = N;
-    g.do_gauge = m.do_gauge;
     g.semantics = m.semantics;
-    g.tol = (T)m.kubo_tol;
     cplx<T>* Vk = V + (size_t)k * 3 * NN;
     // velocity
     for (int e = tid; e < 3 * NN; e += nt) {
@@ -69,7 +73,7 @@ __global__ void __launch_bounds__(256) gauge_kernel(DevModel m, const T* __restr
             cplx<T> ab = g.HA[(size_t)(3 + a) * NN + p * N + q];
             cplx<T> av = ab;
             if (m.semantics == 0 || !m.do_gauge) av = ab + times_i(g.D(a, p, q));
-            T de = Es[q] - Es[p];
+            const T de = (T)(Es[q] - Es[p]);
             v = hb - times_i(de * av);
         }
         Vk[e] = v;
@@ -117,17 +121,20 @@ __global__ void __launch_bounds__(256) gauge_kernel(DevModel m, const T* __restr
 }  // namespace
 
 template <typename T>
-cudaError_t launch_gauge(const DevModel& m, int64_t nk, const T* E, const cplx<T>* HA, const cplx<T>* OD, cplx<T>* V,
-                         T* CSV, cplx<T>* ODH, cudaStream_t s) {
+cudaError_t launch_gauge(const DevModel& m, int64_t nk, const double* E, const cplx<T>* HA, const cplx<T>* OD,
+                         cplx<T>* V, T* CSV, cplx<T>* ODH, cudaStream_t s) {
     if (nk <= 0) return cudaSuccess;
     int threads = m.N <= 16 ? 128 : 256;
-    gauge_kernel<T><<<(unsigned)nk, threads, 0, s>>>(m, E, HA, OD, V, CSV, ODH);
+    const size_t smem = (size_t)m.N * m.N * sizeof(T);
+    cudaError_t e = cudaFuncSetAttribute(gauge_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    gauge_kernel<T><<<(unsigned)nk, threads, smem, s>>>(m, E, HA, OD, V, CSV, ODH);
     return cudaGetLastError();
 }
 
 template cudaError_t launch_gauge<double>(const DevModel&, int64_t, const double*, const cplx<double>*,
                                           const cplx<double>*, cplx<double>*, double*, cplx<double>*, cudaStream_t);
-template cudaError_t launch_gauge<float>(const DevModel&, int64_t, const float*, const cplx<float>*,
+template cudaError_t launch_gauge<float>(const DevModel&, int64_t, const double*, const cplx<float>*,
                                          const cplx<float>*, cplx<float>*, float*, cplx<float>*, cudaStream_t);
 
 }  // namespace mepi

@@ -7,7 +7,9 @@
 //                with C = a_latt (use_cart_velo) or 2*pi*I; 4 blocks without r(R).
 //   W blocks     W[k][blk][n][m]        complex<T>, the Wannier-gauge H, H_a, A_a,
 //                Omega_q per k-point after the tau phase epilogue.
-//   E, U         E[k][n] ascending, U[k][i][n] = component i of eigenvector n.
+//   E, U         E[k][n] ascending, U[k][i][n] = component i of eigenvector n;
+//                the band kernels always read FP64 energies (E64 in the mixed
+//                form, refined against the FP64 H64[k][n][m]).
 //   HA           HA[k][6][n][m]          complex<T>: Hbar_a (a=0..2), Abar_a.
 //   OD           OD[k][3][n]             complex<T>: diag(U^dag Omega_q U).
 //   V            V[k][3][n][m]           complex<T>: velocity matrices.
@@ -113,16 +115,20 @@ struct AccLayout {
 template <typename T>
 cudaError_t launch_ft_simt(const DevModel& m, const KRange& kr, cplx<T>* W, cudaStream_t s);
 template <typename T>
-cudaError_t launch_eig(int N, int64_t nk, const cplx<T>* W, int nbW, T* E, cplx<T>* U, int max_sweeps,
-                       int* sweeps_max, int* flag_cap, double degen_gap, int* redo_flag, cudaStream_t s);
+cudaError_t launch_eig(int N, int64_t nk, const cplx<T>* W, int nbW, const cplx<double>* H64, T* E, cplx<T>* U,
+                       int max_sweeps, int* sweeps_max, int* flag_cap, double degen_gap, int* redo_flag,
+                       cudaStream_t s);
+cudaError_t launch_ft_h64(const DevModel& m, const KRange& kr, cplx<double>* H64, cudaStream_t s);
+cudaError_t launch_refine(int N, int64_t nk, const cplx<double>* H64, cplx<float>* U, double* E64, double degen_gap,
+                          int first_order, int* redo_flag, cudaStream_t s);
 template <typename T>
 cudaError_t launch_rot(const DevModel& m, int64_t nk, const cplx<T>* W, const cplx<T>* U, cplx<T>* HA,
                        cplx<T>* OD, cudaStream_t s);
 template <typename T>
-cudaError_t launch_gauge(const DevModel& m, int64_t nk, const T* E, const cplx<T>* HA, const cplx<T>* OD,
+cudaError_t launch_gauge(const DevModel& m, int64_t nk, const double* E, const cplx<T>* HA, const cplx<T>* OD,
                          cplx<T>* V, T* CSV, cplx<T>* ODH, cudaStream_t s);
 template <typename T>
-cudaError_t launch_bandsum(const DevModel& m, const JobDev& j, int64_t nk, const T* E, const cplx<T>* V,
+cudaError_t launch_bandsum(const DevModel& m, const JobDev& j, int64_t nk, const double* E, const cplx<T>* V,
                            const T* CSV, const int* skip, double* partials, int n_cta, cudaStream_t s);
 cudaError_t launch_reduce(const double* partials, int n_cta, int size, double* out, cudaStream_t s);
 int bandsum_ctas();
