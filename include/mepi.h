@@ -54,8 +54,10 @@ extern "C" {
 /* arithmetic form of the run */
 #define MEPI_PREC_FP64 0   /* all-FP64 plain form */
 #define MEPI_PREC_MIXED 1  /* split-FP16 tensor-core Fourier sums, FP32 per-k
-                              work, FP64 k-sums, FP64 rerun of k-points whose
-                              band gap falls below degen_gap */
+                              work, FP64 k-sums; k-points whose band gap falls
+                              below degen_gap, or whose occupation or kuboTol
+                              decisions lie within the FP32 error of their
+                              threshold, are rerun in FP64 */
 
 typedef struct mepi_ctx mepi_ctx;
 
@@ -95,7 +97,7 @@ typedef struct {
     int64_t chunk_k;           /* k-points per device chunk; 0 = automatic */
     double degen_gap;          /* MEPI_PREC_MIXED only: minimum band gap (Ha)
                                   for the FP32 per-k path; < 0 = default
-                                  (1e-4 eV) */
+                                  (3e-3 Ha) */
 } mepi_job;
 
 /* Unnormalised local sums, like the reference's *_loc arrays

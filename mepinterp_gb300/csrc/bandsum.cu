@@ -54,22 +54,25 @@ __device__ __forceinline__ T warp_sum(T v) {
 template <typename T>
 __global__ void __launch_bounds__(256) bandsum_kernel(DevModel md, JobDev jb, int64_t nk, const double* __restrict__ Eg,
                                                       const cplx<T>* __restrict__ Vg, const T* __restrict__ CSVg,
-                                                      const int* __restrict__ skip, double* __restrict__ partials) {
+                                                      const int* __restrict__ skip, double* __restrict__ partials,
+                                                      int use_tab) {
     extern __shared__ unsigned char smem_raw[];
     const int N = md.N, NN = N * N, ld = N + 1;
     const int nval = jb.nval, nE = jb.nE;
     cplx<T>* Vs = reinterpret_cast<cplx<T>*>(smem_raw);          // [3][N][ld]
-    T* curv = reinterpret_cast<T*>(Vs + 3 * N * ld);              // [9][N]
-    T* icn = curv + 9 * N;                                        // [9][N] Kubo IC per band
+    double* curv = reinterpret_cast<double*>(Vs + 3 * N * ld);    // [9][N] AHC curvature per band (FP64)
+    double* Es = curv + 9 * N;                                    // [kMaxN] energies (FP64)
+    T* icn = reinterpret_cast<T*>(Es + kMaxN);                    // [9][N] Kubo IC per band
     T* lcn = icn + 9 * N;                                         // [9][N] Kubo LC per band
     T* icv = lcn + 9 * N;                                         // [9][kMaxN] Niu IC
     T* lcv = icv + 9 * kMaxN;                                     // [9][kMaxN] Niu LC
     T* Cs = lcv + 9 * kMaxN;                                      // [kMaxN]
-    double* Es = reinterpret_cast<double*>(Cs + kMaxN);           // [kMaxN], 8-byte aligned below
+    T* Dt = Cs + kMaxN;                                           // [N][N] E_a - E_b (difference formed in FP64)
+    T* Iv = Dt + NN;                                              // [N][N] 1 / (E_a - E_b), 0 on the diagonal
     const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nwarps = nt >> 5;
     const AccLayout L{nE, nval};
     double* P = partials + (size_t)blockIdx.x * L.size();
-    const double tol = md.kubo_tol;
+    const T ttol = (T)md.kubo_tol;
 
     for (int64_t k = blockIdx.x; k < nk; k += gridDim.x) {
         if (skip && skip[k]) continue;
@@ -83,45 +86,71 @@ __global__ void __launch_bounds__(256) bandsum_kernel(DevModel md, JobDev jb, in
             Cs[n] = CSVg ? CSVg[(size_t)k * N + n] : (T)0;
         }
         __syncthreads();
+        if (use_tab) {
+            for (int e = tid; e < NN; e += nt) {
+                const int a = e / N, b = e % N;
+                const T d = (T)(Es[a] - Es[b]);
+                Dt[e] = d;
+                Iv[e] = (a == b) ? (T)0 : (T)1 / d;
+            }
+        }
+        __syncthreads();
         auto V = [&](int a, int n, int m) -> cplx<T> { return Vs[(a * N + n) * ld + m]; };
+        // energy differences (formed in FP64) and their inverses: tabulated when
+        // they fit in shared memory, else formed on the fly
+        auto dE = [&](int a, int b) -> T { return use_tab ? Dt[a * N + b] : (T)(Es[a] - Es[b]); };
+        auto iE = [&](int a, int b) -> T {
+            return use_tab ? Iv[a * N + b] : (a == b ? (T)0 : (T)1 / (T)(Es[a] - Es[b]));
+        };
 
         for (int n0 = warp; n0 < N; n0 += nwarps) {
-            const double E0 = Es[n0];
             const bool niu = (n0 < nval) && jb.do_mep;
-            T s_curv[9], s_ic[9], s_lc[9], s_icv[9], s_lcv[9];
+            double s_curv[9];
+            T s_ic[9], s_lc[9], s_icv[9], s_lcv[9];
 #pragma unroll
-            for (int q = 0; q < 9; ++q) s_curv[q] = s_ic[q] = s_lc[q] = s_icv[q] = s_lcv[q] = (T)0;
+            for (int q = 0; q < 9; ++q) {
+                s_curv[q] = 0.0;
+                s_ic[q] = s_lc[q] = s_icv[q] = s_lcv[q] = (T)0;
+            }
             cplx<T> vnn[3];
 #pragma unroll
             for (int c = 0; c < 3; ++c) vnn[c] = V(c, n0, n0);
             for (int n = lane; n < N; n += 32) {
                 if (n == n0) continue;
-                const double d0nd = E0 - Es[n];  // E0 - En in FP64
-                const T d0n = (T)d0nd;
+                const T d0n = dE(n0, n);   // E0 - En
+                const T i0n = iE(n0, n);   // 1 / (E0 - En)
                 cplx<T> vi[3], vk[3];
 #pragma unroll
                 for (int c = 0; c < 3; ++c) { vi[c] = V(c, n0, n); vk[c] = V(c, n, n0); }
-                // AHC: curv(i,j,n0) = -2 Im(V_i(n0,n) V_j(n,n0)) / (En - E0)^2
+                // AHC: curv(i,j,n0) = -2 sum_n Im(V_i(n0,n) V_j(n,n0)) / (En - E0)^2.  The pair term is
+                // formed once from the ordered pair (a,b) = (min, max) and enters band a with + and band
+                // b with -, so two bands of equal occupation cancel exactly in the Fermi contraction.
                 if (jb.do_ahc) {
-                    T inv = (T)1 / (d0n * d0n);
+                    const int a = n0 < n ? n0 : n, b = n0 < n ? n : n0;
+                    const T iab = iE(a, b);
+                    const T w = (n0 < n ? (T)-2 : (T)2) * iab * iab;
+                    cplx<T> va[3], vb[3];
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) { va[c] = V(c, a, b); vb[c] = V(c, b, a); }
 #pragma unroll
                     for (int j = 0; j < 3; ++j)
 #pragma unroll
-                        for (int i = 0; i < 3; ++i) s_curv[i + 3 * j] += (T)-2 * ((vi[i] * vk[j]).im * inv);
+                        for (int i = 0; i < 3; ++i) s_curv[i + 3 * j] += (double)(w * (va[i] * vb[j]).im);
                 }
                 // LC
                 {
                     cplx<T> x[3];
                     cross3(vk, vnn, x);
                     const T den3 = d0n * d0n * d0n;
+                    const T i3 = i0n * i0n * i0n;
                     bool kubo_ok = jb.do_kubo;
-                    bool niu_ok = niu && (fabs(d0nd * d0nd * d0nd) > tol);
+                    bool niu_ok = niu && (fabs(den3) > ttol);
                     if (kubo_ok || niu_ok) {
 #pragma unroll
                         for (int j = 0; j < 3; ++j)
 #pragma unroll
                             for (int i = 0; i < 3; ++i) {
-                                T v = (vi[i] * x[j]).re / den3;
+                                T v = (vi[i] * x[j]).re * i3;
                                 if (kubo_ok) s_lc[i + 3 * j] += v;
                                 if (niu_ok) s_lcv[i + 3 * j] += v;
                             }
@@ -133,23 +162,21 @@ __global__ void __launch_bounds__(256) bandsum_kernel(DevModel md, JobDev jb, in
 #pragma unroll
                     for (int c = 0; c < 3; ++c) g[c] = gv[c] = mk((T)0, (T)0);
                     const T a2 = d0n * d0n;
-                    const double a2d = d0nd * d0nd;
                     for (int m = 0; m < N; ++m) {
                         if (m == n0) continue;
                         cplx<T> vnm[3], vmo[3], x[3];
 #pragma unroll
                         for (int c = 0; c < 3; ++c) { vnm[c] = V(c, n, m); vmo[c] = V(c, m, n0); }
                         cross3(vnm, vmo, x);
-                        const double d0md = E0 - Es[m];
-                        const T b = (T)(1.0 / d0md);
+                        const T b = iE(n0, m);
 #pragma unroll
                         for (int c = 0; c < 3; ++c) g[c] = g[c] + b * x[c];
-                        if (niu && fabs(a2d * d0md) > tol) {
+                        if (niu && fabs(a2 * dE(n0, m)) > ttol) {
 #pragma unroll
                             for (int c = 0; c < 3; ++c) gv[c] = gv[c] + b * x[c];
                         }
                     }
-                    const T ainv = (T)1 / a2;
+                    const T ainv = i0n * i0n;
 #pragma unroll
                     for (int j = 0; j < 3; ++j)
 #pragma unroll
@@ -161,7 +188,8 @@ __global__ void __launch_bounds__(256) bandsum_kernel(DevModel md, JobDev jb, in
             }
 #pragma unroll
             for (int q = 0; q < 9; ++q) {
-                T a = warp_sum(s_curv[q]), b = warp_sum(s_ic[q]), c = warp_sum(s_lc[q]);
+                const double a = warp_sum(s_curv[q]);
+                T b = warp_sum(s_ic[q]), c = warp_sum(s_lc[q]);
                 T d = warp_sum(s_icv[q]), e = warp_sum(s_lcv[q]);
                 if (lane == 0) {
                     curv[q * N + n0] = a;
@@ -185,16 +213,17 @@ __global__ void __launch_bounds__(256) bandsum_kernel(DevModel md, JobDev jb, in
         if (nE >= 64) {
             for (int e = tid; e < nE; e += nt) {
                 const double ef = jb.ef[e];
-                T ne = 0, a[9], ki[9], kl[9], kc = 0;
+                T ne = 0, ki[9], kl[9], kc = 0;
+                double a[9];
 #pragma unroll
-                for (int q = 0; q < 9; ++q) a[q] = ki[q] = kl[q] = 0;
+                for (int q = 0; q < 9; ++q) { a[q] = 0.0; ki[q] = kl[q] = 0; }
                 for (int n = 0; n < N; ++n) {
                     const T f = fd_stat<T>(Es[n], ef, jb.T_kelvin);
                     ne += f;
                     kc += f * Cs[n];
 #pragma unroll
                     for (int q = 0; q < 9; ++q) {
-                        a[q] -= curv[q * N + n] * f;
+                        a[q] -= curv[q * N + n] * (double)f;
                         ki[q] += icn[q * N + n] * f;
                         kl[q] += lcn[q * N + n] * f;
                     }
@@ -215,16 +244,17 @@ __global__ void __launch_bounds__(256) bandsum_kernel(DevModel md, JobDev jb, in
         } else {
             for (int e = warp; e < nE; e += nwarps) {
                 const double ef = jb.ef[e];
-                T ne = 0, a[9], ki[9], kl[9], kc = 0;
+                T ne = 0, ki[9], kl[9], kc = 0;
+                double a[9];
 #pragma unroll
-                for (int q = 0; q < 9; ++q) a[q] = ki[q] = kl[q] = 0;
+                for (int q = 0; q < 9; ++q) { a[q] = 0.0; ki[q] = kl[q] = 0; }
                 for (int n = lane; n < N; n += 32) {
                     const T f = fd_stat<T>(Es[n], ef, jb.T_kelvin);
                     ne += f;
                     kc += f * Cs[n];
 #pragma unroll
                     for (int q = 0; q < 9; ++q) {
-                        a[q] -= curv[q * N + n] * f;
+                        a[q] -= curv[q * N + n] * (double)f;
                         ki[q] += icn[q * N + n] * f;
                         kl[q] += lcn[q * N + n] * f;
                     }
@@ -269,11 +299,10 @@ int bandsum_ctas() {
 }
 
 template <typename T>
-size_t bandsum_smem(int N) {
+size_t bandsum_smem(int N, bool tables) {
     size_t b = 3 * (size_t)N * (N + 1) * sizeof(cplx<T>);
-    b += (27 * (size_t)N + 18 * kMaxN + kMaxN) * sizeof(T);
-    b = (b + 7) & ~(size_t)7;
-    b += kMaxN * sizeof(double);
+    b += (9 * (size_t)N + kMaxN) * sizeof(double);
+    b += (18 * (size_t)N + 18 * kMaxN + kMaxN + (tables ? 2 * (size_t)N * N : 0)) * sizeof(T);
     return (b + 15) & ~(size_t)15;
 }
 
@@ -281,10 +310,11 @@ template <typename T>
 cudaError_t launch_bandsum(const DevModel& m, const JobDev& j, int64_t nk, const double* E, const cplx<T>* V, const T* CSV,
                            const int* skip, double* partials, int n_cta, cudaStream_t s) {
     if (nk <= 0) return cudaSuccess;
-    size_t smem = bandsum_smem<T>(m.N);
+    const bool tables = bandsum_smem<T>(m.N, true) <= 227 * 1024;
+    size_t smem = bandsum_smem<T>(m.N, tables);
     cudaError_t e = cudaFuncSetAttribute(bandsum_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    bandsum_kernel<T><<<n_cta, 256, smem, s>>>(m, j, nk, E, V, CSV, skip, partials);
+    bandsum_kernel<T><<<n_cta, 256, smem, s>>>(m, j, nk, E, V, CSV, skip, partials, tables ? 1 : 0);
     return cudaGetLastError();
 }
 
@@ -299,3 +329,4 @@ template cudaError_t launch_bandsum<float>(const DevModel&, const JobDev&, int64
                                            const float*, const int*, double*, int, cudaStream_t);
 
 }  // namespace mepi
+

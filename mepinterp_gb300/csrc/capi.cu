@@ -76,6 +76,7 @@ struct mepi_ctx {
     TcPlan tc;
     bool ft_simt_only = false;          // MEPI_FT_SIMT=1: FP64 SIMT Fourier sums in the mixed form too
     int first_order = 1;                // MEPI_REFINE_FIRST_ORDER=0: energies-only refinement
+    int refine = 0;                     // MEPI_REFINE=1: FP64 H(k) + FP64 eigenpair refinement
 };
 
 namespace {
@@ -139,7 +140,7 @@ int ensure_chunk(mepi_ctx* ctx, int64_t chunk) {
     CKM(ctx->W.ensure(chunk * ctx->nb * NN * sizeof(cplx<T>)));
     CKM(ctx->E.ensure(chunk * N * sizeof(T)));
     CKM(ctx->E64.ensure(chunk * N * sizeof(double)));
-    if (sizeof(T) == 4) CKM(ctx->H64.ensure(chunk * NN * sizeof(cplx<double>)));
+    if (sizeof(T) == 4 && ctx->refine) CKM(ctx->H64.ensure(chunk * NN * sizeof(cplx<double>)));
     CKM(ctx->U.ensure(chunk * NN * sizeof(cplx<T>)));
     CKM(ctx->HA.ensure(chunk * 6 * NN * sizeof(cplx<T>)));
     CKM(ctx->OD.ensure(chunk * 3 * N * sizeof(cplx<T>)));
@@ -174,13 +175,22 @@ int run_chunk(mepi_ctx* ctx, const KRange& kr, const JobDev* jb, int n_cta, doub
         STAGE(ST_FT, (launch_ft_simt<T>(ctx->dm, kr, ctx->W.as<cplx<T>>(), ctx->stream)));
     }
     double* E64 = ctx->E64.as<double>();
-    if (mixed) {
+    if (mixed && ctx->refine) {
+        // opt-in: FP64 H(k) and FP64 refinement of the FP32 eigenpairs
         cplx<double>* H64 = ctx->H64.as<cplx<double>>();
         STAGE(ST_FTH, launch_ft_h64(ctx->dm, kr, H64, ctx->stream));
         STAGE(ST_EIG, (launch_eig<T>(ctx->N, nk, ctx->W.as<cplx<T>>(), ctx->nb, H64, ctx->E.as<T>(),
                                      ctx->U.as<cplx<T>>(), 40, counters, counters + 2, degen_gap, flags, ctx->stream)));
         STAGE(ST_REFINE, launch_refine(ctx->N, nk, H64, reinterpret_cast<cplx<float>*>(ctx->U.p), E64, degen_gap,
                                        ctx->first_order, flags, ctx->stream));
+    } else if (mixed) {
+        STAGE(ST_EIG, (launch_eig<T>(ctx->N, nk, ctx->W.as<cplx<T>>(), ctx->nb, nullptr, ctx->E.as<T>(),
+                                     ctx->U.as<cplx<T>>(), 40, counters, counters + 2, degen_gap, flags, ctx->stream)));
+        const bool step = jb && !(jb->T_kelvin > kMinTemp);
+        STAGE(ST_REFINE, launch_window_flags(ctx->N, nk, reinterpret_cast<const float*>(ctx->E.p), E64,
+                                             jb && jb->do_mep ? jb->nval : 0, ctx->dm.kubo_tol, 1e-2,
+                                             jb ? jb->nE : 0, jb ? jb->ef : nullptr, step ? 1 : 0, 1e-4, flags,
+                                             ctx->stream));
     } else {
         STAGE(ST_EIG, (launch_eig<T>(ctx->N, nk, ctx->W.as<cplx<T>>(), ctx->nb, nullptr, reinterpret_cast<T*>(E64),
                                      ctx->U.as<cplx<T>>(), 40, counters, counters + 1, degen_gap, flags, ctx->stream)));
@@ -245,7 +255,7 @@ int run_impl(mepi_ctx* ctx, const mepi_job* job, mepi_acc* out) {
     const bool fp64 = job->precision == MEPI_PREC_FP64;
     int64_t chunk = job->chunk_k > 0 ? job->chunk_k : default_chunk(N, ctx->nb, fp64);
     chunk = std::max<int64_t>(1, std::min<int64_t>(chunk, std::max<int64_t>(count, 1)));
-    const double degen_gap = job->degen_gap >= 0 ? job->degen_gap : 1e-4 / kAuToEv;
+    const double degen_gap = job->degen_gap >= 0 ? job->degen_gap : 3e-3;
 
     AccLayout L{job->n_eF, job->valence_bands};
     const int n_cta = bandsum_ctas();
@@ -462,6 +472,8 @@ int mepi_create(mepi_ctx** out, const mepi_model* m) {
     ctx->ft_simt_only = simt_env && simt_env[0] == '1';
     const char* fo_env = std::getenv("MEPI_REFINE_FIRST_ORDER");
     ctx->first_order = (fo_env && fo_env[0] == '0') ? 0 : 1;
+    const char* rf_env = std::getenv("MEPI_REFINE");
+    ctx->refine = (rf_env && rf_env[0] == '1') ? 1 : 0;
     std::vector<double> Rh(3 * (size_t)nR);
     std::memcpy(Rh.data(), m->R_frac, Rh.size() * sizeof(double));
     if (ctx->S.ensure(S.size() * sizeof(cplx<double>)) != cudaSuccess) return fail(MEPI_ERR_NOMEM);

@@ -58,6 +58,42 @@ template <typename T> __host__ __device__ __forceinline__ void fma_cjc(cplx<T>& 
 template <typename T> __host__ __device__ __forceinline__ cplx<T> times_i(cplx<T> a) { return mk(-a.im, a.re); }
 template <typename T> __host__ __device__ __forceinline__ T abs2(cplx<T> a) { return a.re * a.re + a.im * a.im; }
 
+// C = op(A) B for N x N complex matrices in shared memory (row stride ld),
+// op(A) = A (adjA = false) or A^dag (adjA = true).  Each thread computes 2x2
+// output tiles so every shared-memory load feeds two complex multiply-adds.
+// Row/column N (odd N) reads zero padding the caller provides; only i, j < N
+// are written.  The caller synchronises before and after.
+template <typename T, bool adjA>
+__device__ __forceinline__ void smem_cgemm(int N, int ld, const cplx<T>* __restrict__ A, const cplx<T>* __restrict__ B,
+                                           cplx<T>* __restrict__ Cm, int tid, int nt) {
+    const int h = (N + 1) >> 1;
+    for (int t = tid; t < h * h; t += nt) {
+        const int i0 = 2 * (t / h), j0 = 2 * (t % h);
+        cplx<T> c00 = mk((T)0, (T)0), c01 = c00, c10 = c00, c11 = c00;
+        for (int l = 0; l < N; ++l) {
+            cplx<T> a0, a1;
+            if (adjA) {
+                a0 = conjg(A[l * ld + i0]);
+                a1 = conjg(A[l * ld + i0 + 1]);
+            } else {
+                a0 = A[i0 * ld + l];
+                a1 = A[(i0 + 1) * ld + l];
+            }
+            const cplx<T> b0 = B[l * ld + j0], b1 = B[l * ld + j0 + 1];
+            fma_c(c00, a0, b0);
+            fma_c(c01, a0, b1);
+            fma_c(c10, a1, b0);
+            fma_c(c11, a1, b1);
+        }
+        Cm[i0 * ld + j0] = c00;
+        if (j0 + 1 < N) Cm[i0 * ld + j0 + 1] = c01;
+        if (i0 + 1 < N) {
+            Cm[(i0 + 1) * ld + j0] = c10;
+            if (j0 + 1 < N) Cm[(i0 + 1) * ld + j0 + 1] = c11;
+        }
+    }
+}
+
 // Which k-points a launch covers: k = list ? list[i] : k_begin + i * k_stride.
 struct KRange {
     int64_t k_begin, k_stride, count;
@@ -121,6 +157,8 @@ cudaError_t launch_eig(int N, int64_t nk, const cplx<T>* W, int nbW, const cplx<
 cudaError_t launch_ft_h64(const DevModel& m, const KRange& kr, cplx<double>* H64, cudaStream_t s);
 cudaError_t launch_refine(int N, int64_t nk, const cplx<double>* H64, cplx<float>* U, double* E64, double degen_gap,
                           int first_order, int* redo_flag, cudaStream_t s);
+cudaError_t launch_window_flags(int N, int64_t nk, const float* E32, double* E64, int nval, double tol, double mask_eps,
+                                int nE, const double* ef, int step_occ, double fermi_eps, int* flags, cudaStream_t s);
 template <typename T>
 cudaError_t launch_rot(const DevModel& m, int64_t nk, const cplx<T>* W, const cplx<T>* U, cplx<T>* HA,
                        cplx<T>* OD, cudaStream_t s);

@@ -8,9 +8,10 @@
 // curv_gaugeTrafo collapse to 3 diagonal-only rotations here plus O(N^2)
 // commutator diagonals in the gauge kernel.
 //
-// One k-point per CTA: U and the operand are staged in shared memory and each
-// product is an N x N x N complex contraction spread over the CTA's threads
-// (thread (i, j) reads a broadcast row element and a contiguous column run).
+// One k-point per CTA: U and the operand are staged in shared memory (padded
+// to an even size with zeros) and each product is an N x N x N complex
+// contraction in which every thread computes 2 x 2 output tiles
+// (smem_cgemm), so each shared-memory load feeds two multiply-adds.
 // Without the gauge transformation the kernel copies the W-gauge blocks.
 #include "mepi_internal.cuh"
 
@@ -24,9 +25,10 @@ __global__ void __launch_bounds__(256) rot_kernel(DevModel m, const cplx<T>* __r
                                                   cplx<T>* __restrict__ OD) {
     extern __shared__ unsigned char smem_raw[];
     const int N = m.N, NN = N * N;
+    const int Np = N + (N & 1), ld = Np;     // even padded size, zero padding
     cplx<T>* Us = reinterpret_cast<cplx<T>*>(smem_raw);
-    cplx<T>* Xs = Us + NN;
-    cplx<T>* Ts = Xs + NN;
+    cplx<T>* Xs = Us + Np * Np;
+    cplx<T>* Ts = Xs + Np * Np;
     const int tid = threadIdx.x, nt = blockDim.x;
     const int64_t k = blockIdx.x;
     const int nbW = m.nb;
@@ -42,44 +44,35 @@ __global__ void __launch_bounds__(256) rot_kernel(DevModel m, const cplx<T>* __r
                 for (int n = tid; n < N; n += nt) OD[((size_t)k * 3 + q) * N + n] = Wk[(size_t)(7 + q) * NN + n * N + n];
         return;
     }
-    for (int e = tid; e < NN; e += nt) Us[e] = Ug[(size_t)k * NN + e];
+    const cplx<T> zero = mk((T)0, (T)0);
+    for (int e = tid; e < Np * Np; e += nt) {
+        const int i = e / Np, j = e % Np;
+        Us[e] = (i < N && j < N) ? Ug[(size_t)k * NN + i * N + j] : zero;
+        Xs[e] = zero;
+        Ts[e] = zero;
+    }
     // blocks 1..3 (H_a) and 4..6 (A_a): full rotation
     for (int j = 0; j < nmat; ++j) {
         __syncthreads();
-        for (int e = tid; e < NN; e += nt) Xs[e] = Wk[(size_t)(1 + j) * NN + e];
+        for (int e = tid; e < NN; e += nt) Xs[(e / N) * ld + e % N] = Wk[(size_t)(1 + j) * NN + e];
         __syncthreads();
-        // T = X U
-        for (int e = tid; e < NN; e += nt) {
-            int i = e / N, c = e % N;
-            cplx<T> acc = mk((T)0, (T)0);
-            for (int l = 0; l < N; ++l) fma_c(acc, Xs[i * N + l], Us[l * N + c]);
-            Ts[e] = acc;
-        }
+        smem_cgemm<T, false>(N, ld, Xs, Us, Ts, tid, nt);          // T = X U
         __syncthreads();
-        // Y = U^dag T
-        for (int e = tid; e < NN; e += nt) {
-            int i = e / N, c = e % N;
-            cplx<T> acc = mk((T)0, (T)0);
-            for (int l = 0; l < N; ++l) fma_cjc(acc, Us[l * N + i], Ts[l * N + c]);
-            HAk[(size_t)j * NN + e] = acc;
-        }
+        smem_cgemm<T, true>(N, ld, Us, Ts, Xs, tid, nt);           // Y = U^dag T (into Xs)
+        __syncthreads();
+        for (int e = tid; e < NN; e += nt) HAk[(size_t)j * NN + e] = Xs[(e / N) * ld + e % N];
     }
     if (!m.has_r) return;
     // blocks 7..9 (Omega_q): diagonal of U^dag Omega_q U only
     for (int q = 0; q < 3; ++q) {
         __syncthreads();
-        for (int e = tid; e < NN; e += nt) Xs[e] = Wk[(size_t)(7 + q) * NN + e];
+        for (int e = tid; e < NN; e += nt) Xs[(e / N) * ld + e % N] = Wk[(size_t)(7 + q) * NN + e];
         __syncthreads();
-        for (int e = tid; e < NN; e += nt) {
-            int i = e / N, c = e % N;
-            cplx<T> acc = mk((T)0, (T)0);
-            for (int l = 0; l < N; ++l) fma_c(acc, Xs[i * N + l], Us[l * N + c]);
-            Ts[e] = acc;
-        }
+        smem_cgemm<T, false>(N, ld, Xs, Us, Ts, tid, nt);          // T = Omega U
         __syncthreads();
         for (int n = tid; n < N; n += nt) {
-            cplx<T> acc = mk((T)0, (T)0);
-            for (int l = 0; l < N; ++l) fma_cjc(acc, Us[l * N + n], Ts[l * N + n]);
+            cplx<T> acc = zero;
+            for (int l = 0; l < N; ++l) fma_cjc(acc, Us[l * ld + n], Ts[l * ld + n]);
             OD[((size_t)k * 3 + q) * N + n] = acc;
         }
     }
@@ -91,7 +84,8 @@ template <typename T>
 cudaError_t launch_rot(const DevModel& m, int64_t nk, const cplx<T>* W, const cplx<T>* U, cplx<T>* HA, cplx<T>* OD,
                        cudaStream_t s) {
     if (nk <= 0) return cudaSuccess;
-    size_t smem = 3 * (size_t)m.N * m.N * sizeof(cplx<T>);
+    const int Np = m.N + (m.N & 1);
+    size_t smem = 3 * (size_t)Np * Np * sizeof(cplx<T>);
     cudaError_t e = cudaFuncSetAttribute(rot_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     int threads = m.N <= 16 ? 128 : 256;
