@@ -41,6 +41,8 @@ extern "C" {
 #define MEPI_ERR_EIG 4          /* Jacobi eigensolver hit its sweep cap */
 #define MEPI_ERR_NONHERM 5      /* H(R) is not Hermitian: H(-R) != H(R)^dag */
 #define MEPI_ERR_NONFINITE 6    /* NaN/Inf in the input model */
+#define MEPI_ERR_SCRATCH 7      /* mepi_bandsum_noalloc: problem larger than its
+                                   fixed scratch array */
 
 /* semantics where the reference is not reproducible (see mepi_model) */
 #define MEPI_SEM_REF 0
@@ -152,6 +154,38 @@ int mepi_interp_k(mepi_ctx *ctx, int32_t precision, int64_t n_k, const double *k
 
 /* Device time per stage of the last mepi_run. */
 int mepi_get_timing(const mepi_ctx *ctx, mepi_timing *t);
+
+/* Band sums without any device allocation.  No counterpart in the reference.
+ *
+ * For callers that cannot allocate device memory when they need the sums: a
+ * host code that gives all device memory to its own pool at start-up, a job
+ * held to a fixed device-memory budget, or a loop that cannot take the
+ * latency and implicit synchronisation of cudaMalloc.  The caller already
+ * holds, in device memory, the energies and velocity matrices of n_k
+ * k-points (for instance from its own interpolation) and gets back the same
+ * unnormalised sums mepi_run accumulates:
+ *   en_k     device, n_k x n_wf FP64 eigenvalues (ascending per k-point)
+ *   V        device, complex128 as (re, im) pairs, element (k, a, n, m) at
+ *            ((k*3 + a)*n_wf + n)*n_wf + m: the velocity matrices V_ka
+ *   csv      device, n_k x n_wf Chern-Simons per-band values
+ *            0.5 Re(sum_c conj(A_c(n,n)) om_c(n)), or NULL for none
+ *   ef_lst   device, n_eF Fermi energies (Hartree)
+ *   sums     device, 37*n_eF + 27*valence_bands doubles, written (not added to)
+ *            in the order Ne_sum(n_eF), ahc(3,3,n_eF), kubo_mep_ic(3,3,n_eF),
+ *            kubo_mep_lc, kubo_mep_cs, mep_ic(3,3,valence_bands), mep_lc, mep_cs
+ *   stream   a cudaStream_t, or NULL for the default stream; the work is
+ *            enqueued there and the call returns without synchronising.
+ * Its scratch is one fixed 4 MiB device array in the library (held by every
+ * GPU that loads the library until the process exits), used as 152 slices of
+ * 37*n_eF + 27*valence_bands doubles: problems with
+ * 37*n_eF + 27*valence_bands > 3449 are rejected with MEPI_ERR_SCRATCH.  All
+ * calls share that array, so calls whose work overlaps on the GPU (on
+ * different streams, or from several host threads) race; serialise them.  The
+ * first call on each device looks up the array's device address; make that
+ * first call before capturing any stream. */
+int mepi_bandsum_noalloc(int32_t n_wf, int64_t n_k, const double *en_k, const double *V, const double *csv,
+                         int32_t n_eF, const double *ef_lst, double T_kelvin, int32_t valence_bands,
+                         uint32_t outputs, double kubo_tol, double *sums, void *stream);
 
 /* Frees the context and its device memory. */
 int mepi_destroy(mepi_ctx *ctx);

@@ -21,6 +21,9 @@
 // Fermi energy.  A CTA owns one FP64 accumulator slice for its whole k stripe
 // (k = blockIdx.x, blockIdx.x + gridDim.x, ...), so the final reduction over
 // slices runs in a fixed order and the result is deterministic.
+#include <mutex>
+
+#include "../../include/mepi.h"
 #include "mepi_internal.cuh"
 
 namespace mepi {
@@ -330,3 +333,79 @@ template cudaError_t launch_bandsum<float>(const DevModel&, const JobDev&, int64
 
 }  // namespace mepi
 
+// ---------------------------------------------------------------------------
+// Allocation-free variant of the band sums (mepi_bandsum_noalloc).
+//
+// Some callers of this library cannot allocate device memory at the moment
+// they want the band sums: a host code that hands every byte of device memory
+// to its own pool at start-up and forbids later allocations, a job confined to
+// a fixed device-memory budget where a late cudaMalloc may fail, or a loop that
+// cannot afford cudaMalloc's latency and implicit synchronisation.  For them
+// this entry point keeps its only scratch -- the per-CTA FP64 partial sums --
+// in a file-scope device array of fixed size instead of a cudaMalloc'd buffer;
+// the caller passes device pointers for every input and output.
+namespace mepi {
+namespace {
+constexpr size_t kNoAllocDoubles = size_t(1) << 19;  // 4 MiB of FP64 partial sums
+constexpr int kNoAllocCtas = 152;                     // CTAs (slices) of the variant
+constexpr int kMaxDevices = 64;
+static __device__ __align__(256) double g_noalloc_partials[kNoAllocDoubles];
+
+std::mutex g_noalloc_mu;
+double* g_noalloc_ptr[kMaxDevices] = {};
+
+// Device address of the scratch array on the current device, looked up once
+// per device (the host-side symbol is only a stand-in, not a device address).
+cudaError_t noalloc_scratch(double** out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_noalloc_partials);
+        if (e != cudaSuccess) return e;
+        g_noalloc_ptr[dev] = static_cast<double*>(p);
+    }
+    *out = g_noalloc_ptr[dev];
+    return cudaSuccess;
+}
+}  // namespace
+
+}  // namespace mepi
+
+extern "C" int mepi_bandsum_noalloc(int32_t n_wf, int64_t n_k, const double* en_k, const double* V,
+                                    const double* csv, int32_t n_eF, const double* ef_lst, double T_kelvin,
+                                    int32_t valence_bands, uint32_t outputs, double kubo_tol, double* sums,
+                                    void* stream) {
+    using namespace mepi;
+    if (n_wf <= 0 || n_wf > kMaxN || n_k < 0 || n_eF <= 0 || valence_bands < 0 || valence_bands > n_wf)
+        return MEPI_ERR_ARG;
+    if (!ef_lst || !sums || (n_k > 0 && (!en_k || !V))) return MEPI_ERR_ARG;
+    if (!(kubo_tol >= 0.0) || !(T_kelvin == T_kelvin)) return MEPI_ERR_ARG;
+    const AccLayout L{n_eF, valence_bands};
+    if ((size_t)kNoAllocCtas * (size_t)L.size() > kNoAllocDoubles) return MEPI_ERR_SCRATCH;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    double* scratch = nullptr;
+    if (noalloc_scratch(&scratch) != cudaSuccess) return MEPI_ERR_CUDA;
+    // the array keeps the previous call's sums: clear this call's slices
+    if (cudaMemsetAsync(scratch, 0, (size_t)kNoAllocCtas * L.size() * sizeof(double), s) != cudaSuccess)
+        return MEPI_ERR_CUDA;
+    DevModel md{};
+    md.N = n_wf;
+    md.kubo_tol = kubo_tol;
+    JobDev jb{};
+    jb.nE = n_eF;
+    jb.nval = valence_bands;
+    jb.do_ahc = (outputs & MEPI_OUT_AHC) ? 1 : 0;
+    jb.do_mep = (outputs & MEPI_OUT_MEP_NIU) ? 1 : 0;
+    jb.do_kubo = (outputs & MEPI_OUT_KUBO_MEP) ? 1 : 0;
+    jb.T_kelvin = T_kelvin;
+    jb.ef = ef_lst;
+    if (launch_bandsum<double>(md, jb, n_k, en_k, reinterpret_cast<const cplx<double>*>(V), csv, nullptr, scratch,
+                               kNoAllocCtas, s) != cudaSuccess)
+        return MEPI_ERR_CUDA;
+    if (launch_reduce(scratch, kNoAllocCtas, L.size(), sums, s) != cudaSuccess) return MEPI_ERR_CUDA;
+    return MEPI_OK;
+}

@@ -381,6 +381,7 @@ const char* mepi_strerror(int s) {
         case MEPI_ERR_EIG: return "Jacobi eigensolver reached its sweep limit";
         case MEPI_ERR_NONHERM: return "H(R) is not Hermitian (H(-R) != H(R)^dag or -R missing)";
         case MEPI_ERR_NONFINITE: return "NaN or Inf in the model";
+        case MEPI_ERR_SCRATCH: return "problem larger than the fixed scratch array of mepi_bandsum_noalloc";
         default: return "unknown status";
     }
 }

@@ -1,0 +1,89 @@
+"""GPU test of mepi_bandsum_noalloc, the entry point that allocates nothing.
+
+It exists for callers that cannot allocate device memory when they want the
+band sums (all device memory handed to their own pool at start-up, a fixed
+device-memory budget, or no room for cudaMalloc's latency and implicit
+synchronisation).  The test holds the inputs and outputs in caller-owned
+device buffers, calls the entry point through the C ABI twice in a row, and
+checks both results against mepi_run's sums over the same k-points, within
+the 1e-8 relative tolerance of the FP64 parity tests.  It also checks that a
+problem larger than the fixed scratch array is rejected.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from mepinterp_gb300 import api
+from mepinterp_gb300.generator import random_tb_model
+from oracle import ref_numpy as O
+
+pytestmark = pytest.mark.gpu
+
+SUM_TOL = 1e-8
+ERR_SCRATCH = 7
+
+
+def _bind(lib):
+    f = lib.mepi_bandsum_noalloc
+    f.argtypes = [C.c_int32, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_double,
+                  C.c_int32, C.c_uint32, C.c_double, C.c_void_p, C.c_void_p]
+    f.restype = C.c_int
+    return f
+
+
+def _csv(A, Om):
+    """0.5 Re(sum_c conj(A_c(n,n)) om_c(n)), om_c = sum_ab eps_abc Om_ab."""
+    om = np.stack([Om[:, 1, 2] - Om[:, 2, 1], Om[:, 2, 0] - Om[:, 0, 2], Om[:, 0, 1] - Om[:, 1, 0]], axis=1)
+    return 0.5 * np.einsum("kcn,kcn->kn", np.conj(A), om).real
+
+
+def _rel(a, b):
+    scale = np.abs(b).max()
+    return float(np.abs(a - b).max() / scale) if scale > 0 else float(np.abs(a).max())
+
+
+def test_noalloc_matches_mepi_run(gpu_lib):
+    import torch
+    fn = _bind(gpu_lib)
+    model = random_tb_model(n_wf=8, r_max=1, seed=1)
+    mp = (4, 4, 4)
+    ef = np.array([-0.02, 0.0, 0.01])
+    nval, N = 4, 8
+    job = dict(mp_grid=mp, ef_lst=ef, T_kelvin=300.0, valence_bands=nval)
+    kpts = O.rel_kpts(mp, np.arange(64))
+    with api.Context(model) as ctx:
+        E, V, A, Om = ctx.get_wann_interp(kpts, precision=api.PREC_FP64)
+        ref = ctx.core_worker_loc(job, precision=api.PREC_FP64)
+    dev = torch.device("cuda:0")
+    d_E = torch.from_numpy(np.ascontiguousarray(E)).to(dev)
+    d_V = torch.from_numpy(np.ascontiguousarray(V).view(np.float64)).to(dev)   # [k][a][n][m] (re, im)
+    d_csv = torch.from_numpy(np.ascontiguousarray(_csv(A, Om))).to(dev)
+    d_ef = torch.from_numpy(ef).to(dev)
+    size = 37 * ef.size + 27 * nval
+    stream = torch.cuda.current_stream(dev).cuda_stream
+    for _call in range(2):
+        d_sums = torch.full((size,), np.nan, dtype=torch.float64, device=dev)
+        rc = fn(N, 64, d_E.data_ptr(), d_V.data_ptr(), d_csv.data_ptr(), ef.size, d_ef.data_ptr(), 300.0, nval,
+                7, 1e-5, d_sums.data_ptr(), C.c_void_p(stream))
+        assert rc == 0, gpu_lib.mepi_strerror(rc)
+        torch.cuda.synchronize()
+        s = d_sums.cpu().numpy()
+        nE = ef.size
+        got = {"Ne_sum": s[:nE], "ahc": s[nE:10 * nE], "kubo_mep_ic": s[10 * nE:19 * nE],
+               "kubo_mep_lc": s[19 * nE:28 * nE], "kubo_mep_cs": s[28 * nE:37 * nE],
+               "mep_ic": s[37 * nE:37 * nE + 9 * nval], "mep_lc": s[37 * nE + 9 * nval:37 * nE + 18 * nval],
+               "mep_cs": s[37 * nE + 18 * nval:]}
+        for k, v in got.items():
+            r = np.asarray(ref[k]).ravel(order="F")
+            assert _rel(v, r) < SUM_TOL, (k, _rel(v, r))
+
+
+def test_noalloc_rejects_oversized_problem(gpu_lib):
+    import torch
+    fn = _bind(gpu_lib)
+    dev = torch.device("cuda:0")
+    d = torch.zeros(1024, dtype=torch.float64, device=dev)
+    # 37 * 100 + 27 * 4 > 3449: beyond the fixed scratch array
+    rc = fn(8, 1, d.data_ptr(), d.data_ptr(), None, 100, d.data_ptr(), 0.0, 4, 7, 1e-5, d.data_ptr(), None)
+    assert rc == ERR_SCRATCH
