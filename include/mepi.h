@@ -122,7 +122,7 @@ typedef struct {
 /* Device time of each stage of the last mepi_run (CUDA events on the
  * library's stream), milliseconds, with launch counts. */
 typedef struct {
-    double ft_ms;              /* Fourier sums (SIMT FP64 or tensor-core GEMM) */
+    double ft_ms;              /* Fourier sums (separable, SIMT FP64 or tensor-core GEMM) */
     double phase_ms;           /* mixed form: phase-operand generation */
     double fth_ms;             /* mixed form: FP64 Fourier sum of H(k) alone */
     double eig_ms;             /* Jacobi eigensolver */
@@ -135,6 +135,8 @@ typedef struct {
     int64_t n_k;               /* k-points of the run */
     int64_t h2d_bytes;         /* host->device bytes since mepi_create */
     int64_t d2h_bytes;         /* device->host bytes since mepi_create */
+    double plan_ms;            /* host wall time building the separable-sum slabs
+                                  (0 when a run reuses the slabs of its mesh) */
 } mepi_timing;
 
 /* Replaces read_tb_basis's arrays being handed to get_wann_interp

@@ -69,7 +69,7 @@ class MepiTiming(C.Structure):
     _fields_ = ([(f"{s}_ms", C.c_double) for s in ("ft", "phase", "fth", "eig", "refine", "rot", "gauge",
                                                    "bandsum", "reduce", "total", "run")]
                 + [(f"{s}_launches", C.c_int32) for s in STAGES]
-                + [("n_k", C.c_int64), ("h2d_bytes", C.c_int64), ("d2h_bytes", C.c_int64)])
+                + [("n_k", C.c_int64), ("h2d_bytes", C.c_int64), ("d2h_bytes", C.c_int64), ("plan_ms", C.c_double)])
 
 
 _lib: Optional[C.CDLL] = None

@@ -13,6 +13,7 @@
 //              smallest band gap is below degen_gap is skipped there and rerun
 //              through the FP64 pipeline afterwards.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -74,9 +75,15 @@ struct mepi_ctx {
     int64_t h2d = 0, d2h = 0;           // host<->device byte counters
     std::vector<cplx<double>> S_host;  // FP64 stack, kept to build the tensor-core operands
     TcPlan tc;
-    bool ft_simt_only = false;          // MEPI_FT_SIMT=1: FP64 SIMT Fourier sums in the mixed form too
-    int first_order = 1;                // MEPI_REFINE_FIRST_ORDER=0: energies-only refinement
-    int refine = 0;                     // MEPI_REFINE=1: FP64 H(k) + FP64 eigenpair refinement
+    int ft_pref = 0;                    // MEPI_FT: 0 auto (separable when possible), 1 tensor core, 2 SIMT
+    std::vector<double> R_host;         // lattice vectors, kept for the separable plan
+    SepPlan sep;                        // separable-sum slabs of the current mesh
+    bool sep_active = false;            // this run's chunks take the separable sums
+    double plan_ms = 0.0;
+    // k-points of the run in (qx, qy)-column order, for slab reuse
+    DevBuf kcol;
+    std::vector<int64_t> kcol_host;
+    int64_t kcol_key[6] = {-1, -1, -1, -1, -1, -1};
 };
 
 namespace {
@@ -140,7 +147,7 @@ int ensure_chunk(mepi_ctx* ctx, int64_t chunk) {
     CKM(ctx->W.ensure(chunk * ctx->nb * NN * sizeof(cplx<T>)));
     CKM(ctx->E.ensure(chunk * N * sizeof(T)));
     CKM(ctx->E64.ensure(chunk * N * sizeof(double)));
-    if (sizeof(T) == 4 && ctx->refine) CKM(ctx->H64.ensure(chunk * NN * sizeof(cplx<double>)));
+    if (sizeof(T) == 4) CKM(ctx->H64.ensure(chunk * NN * sizeof(cplx<double>)));
     CKM(ctx->U.ensure(chunk * NN * sizeof(cplx<T>)));
     CKM(ctx->HA.ensure(chunk * 6 * NN * sizeof(cplx<T>)));
     CKM(ctx->OD.ensure(chunk * 3 * N * sizeof(cplx<T>)));
@@ -161,7 +168,10 @@ int run_chunk(mepi_ctx* ctx, const KRange& kr, const JobDev* jb, int n_cta, doub
     int* counters = ctx->counters.as<int>();
     const bool mixed = sizeof(T) == 4;
     int* flags = want_flags ? ctx->flags.as<int>() : nullptr;
-    if (mixed && !ctx->ft_simt_only) {
+    const bool sep = ctx->sep_active && !kr.kpts && (mixed || ctx->sep.fp64);
+    if (sep) {
+        STAGE(ST_FT, (launch_sep_w<T>(ctx->sep, ctx->dm, kr, ctx->W.as<cplx<T>>(), ctx->stream)));
+    } else if (mixed && ctx->ft_pref != 2) {
         if (!ctx->tc.ready()) {
             int rc = tc_plan_init(ctx->tc, ctx->dm, ctx->S_host.data());
             if (rc) return rc;
@@ -175,22 +185,17 @@ int run_chunk(mepi_ctx* ctx, const KRange& kr, const JobDev* jb, int n_cta, doub
         STAGE(ST_FT, (launch_ft_simt<T>(ctx->dm, kr, ctx->W.as<cplx<T>>(), ctx->stream)));
     }
     double* E64 = ctx->E64.as<double>();
-    if (mixed && ctx->refine) {
-        // opt-in: FP64 H(k) and FP64 refinement of the FP32 eigenpairs
+    if (mixed) {
+        // FP64 H(k), FP32 Jacobi on it, FP64 residual refinement of the eigenpairs
         cplx<double>* H64 = ctx->H64.as<cplx<double>>();
-        STAGE(ST_FTH, launch_ft_h64(ctx->dm, kr, H64, ctx->stream));
+        if (sep)
+            STAGE(ST_FTH, launch_sep_h64(ctx->sep, kr, H64, ctx->stream));
+        else
+            STAGE(ST_FTH, launch_ft_h64(ctx->dm, kr, H64, ctx->stream));
         STAGE(ST_EIG, (launch_eig<T>(ctx->N, nk, ctx->W.as<cplx<T>>(), ctx->nb, H64, ctx->E.as<T>(),
                                      ctx->U.as<cplx<T>>(), 40, counters, counters + 2, degen_gap, flags, ctx->stream)));
-        STAGE(ST_REFINE, launch_refine(ctx->N, nk, H64, reinterpret_cast<cplx<float>*>(ctx->U.p), E64, degen_gap,
-                                       ctx->first_order, flags, ctx->stream));
-    } else if (mixed) {
-        STAGE(ST_EIG, (launch_eig<T>(ctx->N, nk, ctx->W.as<cplx<T>>(), ctx->nb, nullptr, ctx->E.as<T>(),
-                                     ctx->U.as<cplx<T>>(), 40, counters, counters + 2, degen_gap, flags, ctx->stream)));
-        const bool step = jb && !(jb->T_kelvin > kMinTemp);
-        STAGE(ST_REFINE, launch_window_flags(ctx->N, nk, reinterpret_cast<const float*>(ctx->E.p), E64,
-                                             jb && jb->do_mep ? jb->nval : 0, ctx->dm.kubo_tol, 1e-2,
-                                             jb ? jb->nE : 0, jb ? jb->ef : nullptr, step ? 1 : 0, 1e-4, flags,
-                                             ctx->stream));
+        STAGE(ST_REFINE, launch_refine(ctx->N, nk, H64, reinterpret_cast<const float*>(ctx->E.p),
+                                       reinterpret_cast<cplx<float>*>(ctx->U.p), E64, degen_gap, flags, ctx->stream));
     } else {
         STAGE(ST_EIG, (launch_eig<T>(ctx->N, nk, ctx->W.as<cplx<T>>(), ctx->nb, nullptr, reinterpret_cast<T*>(E64),
                                      ctx->U.as<cplx<T>>(), 40, counters, counters + 1, degen_gap, flags, ctx->stream)));
@@ -229,6 +234,7 @@ int collect_timing(mepi_ctx* ctx, int64_t nk) {
                  t.reduce_ms;
     t.h2d_bytes = ctx->h2d;
     t.d2h_bytes = ctx->d2h;
+    t.plan_ms = ctx->plan_ms;
     ctx->timing = t;
     return 0;
 }
@@ -240,6 +246,49 @@ int64_t default_chunk(int N, int nb, bool fp64) {
     c = std::min<int64_t>(c, fp64 ? 16384 : 65536);
     c = std::max<int64_t>(64, c & ~(int64_t)63);
     return c;
+}
+
+// Separable sums for this run when the model, mesh and memory allow them:
+// builds (or reuses) the slabs and the (qx, qy)-column ordered k list.
+int prepare_sep(mepi_ctx* ctx, const mepi_job* job, int64_t count, bool fp64) {
+    ctx->sep_active = false;
+    ctx->plan_ms = 0.0;
+    if (ctx->ft_pref != 0 || count <= 0) return 0;
+    const int mp[3] = {job->mp_grid[0], job->mp_grid[1], job->mp_grid[2]};
+    const bool reuse = ctx->sep.ready && ctx->sep.fp64 == fp64 && ctx->sep.mp[0] == mp[0] && ctx->sep.mp[1] == mp[1] &&
+                       ctx->sep.mp[2] == mp[2];
+    if (!reuse) {
+        const auto t0 = std::chrono::steady_clock::now();
+        int rc = sep_plan_build(ctx->sep, ctx->dm, ctx->R_host.data(), ctx->S_host.data(), mp, fp64, ctx->stream);
+        if (rc == 1) return 0;
+        if (rc) {
+            cudaGetLastError();
+            return rc;
+        }
+        ctx->h2d += ctx->sep.h2d_bytes;
+        ctx->plan_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    }
+    const int64_t key[6] = {mp[0], mp[1], mp[2], job->k_begin, job->k_stride, count};
+    if (!std::equal(key, key + 6, ctx->kcol_key)) {
+        std::vector<int64_t> L;
+        L.reserve(count);
+        const int64_t M = (int64_t)mp[0] * mp[1];
+        for (int qx = 0; qx < mp[0]; ++qx)
+            for (int qy = 0; qy < mp[1]; ++qy)
+                for (int qz = 0; qz < mp[2]; ++qz) {
+                    const int64_t d = qx + (int64_t)mp[0] * qy + M * qz - job->k_begin;
+                    if (d >= 0 && d % job->k_stride == 0 && d / job->k_stride < count) L.push_back(d + job->k_begin);
+                }
+        if ((int64_t)L.size() != count) return MEPI_ERR_ARG;
+        CKM(ctx->kcol.ensure(L.size() * sizeof(int64_t)));
+        CK(cudaMemcpyAsync(ctx->kcol.p, L.data(), L.size() * sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+        ctx->h2d += L.size() * sizeof(int64_t);
+        ctx->kcol_host.swap(L);
+        std::copy(key, key + 6, ctx->kcol_key);
+    }
+    ctx->sep_active = true;
+    return 0;
 }
 
 int run_impl(mepi_ctx* ctx, const mepi_job* job, mepi_acc* out) {
@@ -281,12 +330,22 @@ int run_impl(mepi_ctx* ctx, const mepi_job* job, mepi_acc* out) {
 
     std::vector<int64_t> redo;
     int rc = 0;
+    rc = prepare_sep(ctx, job, count, fp64);
+    if (rc) return rc;
+    // chunk c0..c0+cn of the run's k-points: the column-ordered list, or the
+    // rank's stride
+    auto chunk_range = [&](int64_t c0, int64_t cn) {
+        if (ctx->sep_active)
+            return KRange{0, 1, cn, ctx->kcol.as<int64_t>() + c0, nullptr,
+                          {job->mp_grid[0], job->mp_grid[1], job->mp_grid[2]}};
+        return KRange{job->k_begin + c0 * job->k_stride, job->k_stride, cn, nullptr, nullptr,
+                      {job->mp_grid[0], job->mp_grid[1], job->mp_grid[2]}};
+    };
     if (fp64) {
         rc = ensure_chunk<double>(ctx, chunk);
         if (rc) return rc;
         for (int64_t c0 = 0; c0 < count; c0 += chunk) {
-            KRange kr{job->k_begin + c0 * job->k_stride, job->k_stride, std::min(chunk, count - c0), nullptr, nullptr,
-                      {job->mp_grid[0], job->mp_grid[1], job->mp_grid[2]}};
+            KRange kr = chunk_range(c0, std::min(chunk, count - c0));
             rc = run_chunk<double>(ctx, kr, &jb, n_cta, 0.0, false, true, nullptr);
             if (rc) return rc;
         }
@@ -303,8 +362,7 @@ int run_impl(mepi_ctx* ctx, const mepi_job* job, mepi_acc* out) {
         }
         for (int64_t ci = 0; ci < nchunks; ++ci) {
             int64_t c0 = ci * chunk, cn = std::min(chunk, count - c0);
-            KRange kr{job->k_begin + c0 * job->k_stride, job->k_stride, cn, nullptr, nullptr,
-                      {job->mp_grid[0], job->mp_grid[1], job->mp_grid[2]}};
+            KRange kr = chunk_range(c0, cn);
             rc = run_chunk<float>(ctx, kr, &jb, n_cta, degen_gap, true, true, nullptr);
             if (rc) return rc;
             CK(cudaMemcpyAsync(ctx->h_flags + c0, ctx->flags.p, cn * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
@@ -312,7 +370,7 @@ int run_impl(mepi_ctx* ctx, const mepi_job* job, mepi_acc* out) {
         }
         CK(cudaStreamSynchronize(ctx->stream));
         for (int64_t i = 0; i < count; ++i)
-            if (ctx->h_flags[i]) redo.push_back(job->k_begin + i * job->k_stride);
+            if (ctx->h_flags[i]) redo.push_back(ctx->sep_active ? ctx->kcol_host[i] : job->k_begin + i * job->k_stride);
         if (!redo.empty()) {
             int64_t rchunk = std::min<int64_t>(default_chunk(N, ctx->nb, true), (int64_t)redo.size());
             rc = ensure_chunk<double>(ctx, rchunk);
@@ -469,12 +527,11 @@ int mepi_create(mepi_ctx** out, const mepi_model* m) {
                 }
             }
     }
-    const char* simt_env = std::getenv("MEPI_FT_SIMT");
-    ctx->ft_simt_only = simt_env && simt_env[0] == '1';
-    const char* fo_env = std::getenv("MEPI_REFINE_FIRST_ORDER");
-    ctx->first_order = (fo_env && fo_env[0] == '0') ? 0 : 1;
-    const char* rf_env = std::getenv("MEPI_REFINE");
-    ctx->refine = (rf_env && rf_env[0] == '1') ? 1 : 0;
+    // MEPI_FT=tc or =simt forces the tensor-core or SIMT Fourier sums (tests of
+    // the non-separable paths); the default takes the separable sums when the
+    // model and mesh allow them
+    const char* ft_env = std::getenv("MEPI_FT");
+    ctx->ft_pref = (ft_env && std::strcmp(ft_env, "tc") == 0) ? 1 : (ft_env && std::strcmp(ft_env, "simt") == 0) ? 2 : 0;
     std::vector<double> Rh(3 * (size_t)nR);
     std::memcpy(Rh.data(), m->R_frac, Rh.size() * sizeof(double));
     if (ctx->S.ensure(S.size() * sizeof(cplx<double>)) != cudaSuccess) return fail(MEPI_ERR_NOMEM);
@@ -483,6 +540,7 @@ int mepi_create(mepi_ctx** out, const mepi_model* m) {
         return fail(MEPI_ERR_CUDA);
     ctx->h2d += S.size() * sizeof(cplx<double>) + Rh.size() * sizeof(double);
     ctx->S_host.swap(S);
+    ctx->R_host = Rh;
     if (cudaMemcpy(ctx->R.p, Rh.data(), Rh.size() * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess)
         return fail(MEPI_ERR_CUDA);
     if (m->wf_centers) {
@@ -650,6 +708,7 @@ int mepi_destroy(mepi_ctx* ctx) {
     }
     if (ctx->h_flags) cudaFreeHost(ctx->h_flags);
     tc_plan_free(ctx->tc);
+    sep_plan_free(ctx->sep);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return MEPI_OK;

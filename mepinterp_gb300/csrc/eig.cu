@@ -317,148 +317,148 @@ cudaError_t launch_eig(int N, int64_t nk, const cplx<T>* W, int nbW, const cplx<
     return cudaGetLastError();
 }
 
-// FP64 refinement of FP32 eigenpairs against the FP64 H(k):
-//   T = H U, H' = U^dag T (both FP64), E_n = Re H'_nn (Rayleigh quotients, whose
-//   error is second order in the FP32 eigenvector error), and, when first_order
-//   is set, U <- U (1 + X) with X_mn = H'_mn / (E_n - E_m) for the pairs whose
-//   gap exceeds degen_gap.  A k-point with a gap at or below degen_gap, or with
-//   non-finite values, is flagged for the full FP64 rerun.  Eigenpairs are
-//   re-sorted by the refined energies.
+// FP64 refinement of the FP32 eigenpairs (U, lambda) against the FP64 H(k),
+// in residual form so that a single product runs in FP64:
+//   R = H U - U diag(lambda)                 FP64 (the only cancelling product)
+//   P = U^dag R                              FP32 (R is small: its rounding is
+//                                            relative to |R|, not to |H|)
+//   rho_n = lambda_n + P_nn / S_nn,  S_nn = |u_n|^2      (normalised Rayleigh
+//                                            quotient, FP64)
+//   E_n = rho_n + sum_{m!=n} |P_mn|^2 / (rho_n - rho_m)  (second order)
+//   C_mn = P_mn / (rho_n - rho_m),  U' = (U + U C) diag(S_nn)^-1/2    (FP32)
+// C fixes both the eigenvector error and the loss of orthogonality of the
+// warm-started FP32 vectors to first order: <u'_m|u'_n> = S_mn + C_mn +
+// conj(C_nm) + O(2nd) = O(2nd).  The energies are then exact to third order
+// in |P| / gap and the vectors to second order, for any gap above degen_gap.
+// A k-point with a gap at or below degen_gap, an unconverged FP32 Jacobi run
+// (flag already set) or non-finite values is flagged for the full FP64 rerun.
+// Eigenpairs are re-sorted by the refined energies.
 __global__ void __launch_bounds__(256) refine_kernel(int N, const cplx<double>* __restrict__ H64,
-                                                     cplx<float>* __restrict__ U, double* __restrict__ E64,
-                                                     double degen_gap, int first_order, int* __restrict__ redo_flag) {
+                                                     const float* __restrict__ lam, cplx<float>* __restrict__ U,
+                                                     double* __restrict__ E64, double degen_gap,
+                                                     int* __restrict__ redo_flag) {
     extern __shared__ unsigned char smem_raw[];
-    const int NN = N * N;
+    const int Np = N + (N & 1), NPP = Np * Np, h = Np / 2;
     cplx<double>* Hs = reinterpret_cast<cplx<double>*>(smem_raw);
-    cplx<double>* Us = Hs + NN;
-    cplx<double>* Ts = Us + NN;
-    double* Ev = reinterpret_cast<double*>(Ts + NN);
+    double* rho = reinterpret_cast<double*>(Hs + NPP);
+    double* En = rho + Np;
+    double* Sn = En + Np;
+    cplx<float>* Us = reinterpret_cast<cplx<float>*>(Sn + Np);
+    cplx<float>* Rs = Us + NPP;
+    cplx<float>* Ps = Rs + NPP;
+    __shared__ float ls[kMaxN];
     __shared__ int s_flag;
     const int tid = threadIdx.x, nt = blockDim.x;
     const int64_t k = blockIdx.x;
-    for (int e = tid; e < NN; e += nt) {
-        int i = e / N, j = e % N;
-        int a = i < j ? i : j, b = i < j ? j : i;
-        cplx<double> h = H64[(size_t)k * NN + a * N + b];
-        Hs[e] = (i < j) ? h : (i > j) ? conjg(h) : mk(h.re, 0.0);
-        const cplx<float> u = U[(size_t)k * NN + e];
-        Us[e] = mk((double)u.re, (double)u.im);
+    const int NN = N * N;
+    for (int e = tid; e < NPP; e += nt) {
+        const int i = e / Np, j = e % Np;
+        cplx<double> hv = mk(0.0, 0.0);
+        cplx<float> uv = mk(0.f, 0.f);
+        if (i < N && j < N) {
+            const int a = i < j ? i : j, b = i < j ? j : i;
+            const cplx<double> x = H64[(size_t)k * NN + a * N + b];
+            hv = (i < j) ? x : (i > j) ? conjg(x) : mk(x.re, 0.0);
+            uv = U[(size_t)k * NN + i * N + j];
+        }
+        Hs[e] = hv;
+        Us[e] = uv;
     }
+    for (int n = tid; n < Np; n += nt) ls[n] = n < N ? lam[(size_t)k * N + n] : 0.f;
     if (tid == 0) s_flag = redo_flag ? redo_flag[k] : 0;
     __syncthreads();
-    // T = H U
-    for (int e = tid; e < NN; e += nt) {
-        int i = e / N, c = e % N;
-        cplx<double> acc = mk(0.0, 0.0);
-        for (int l = 0; l < N; ++l) fma_c(acc, Hs[i * N + l], Us[l * N + c]);
-        Ts[e] = acc;
-    }
-    __syncthreads();
-    // H' = U^dag T  (into Hs)
-    for (int e = tid; e < NN; e += nt) {
-        int i = e / N, c = e % N;
-        cplx<double> acc = mk(0.0, 0.0);
-        for (int l = 0; l < N; ++l) fma_cjc(acc, Us[l * N + i], Ts[l * N + c]);
-        Hs[e] = acc;
-    }
-    __syncthreads();
-    for (int n = tid; n < N; n += nt) Ev[n] = Hs[n * N + n].re;
-    __syncthreads();
-    // flag near degeneracies (and non-finite energies)
-    for (int e = tid; e < NN; e += nt) {
-        int i = e / N, j = e % N;
-        if (i < j && !(fabs(Ev[i] - Ev[j]) > degen_gap)) s_flag = 1;
-    }
-    if (first_order) {
-        // X into Ts, then U' = U + U X into Hs
-        for (int e = tid; e < NN; e += nt) {
-            int m = e / N, n = e % N;
-            const double d = Ev[n] - Ev[m];
-            Ts[e] = (m != n && fabs(d) > degen_gap) ? mk(Hs[e].re / d, Hs[e].im / d) : mk(0.0, 0.0);
+    // R = H U - U diag(lambda): FP64 accumulation, 2 x 2 tiles per thread
+    for (int t = tid; t < h * h; t += nt) {
+        const int i = 2 * (t / h), c = 2 * (t % h);
+        cplx<double> a00 = mk(0.0, 0.0), a01 = a00, a10 = a00, a11 = a00;
+        for (int l = 0; l < Np; ++l) {
+            const cplx<double> h0 = Hs[i * Np + l], h1 = Hs[(i + 1) * Np + l];
+            const cplx<float> u0f = Us[l * Np + c], u1f = Us[l * Np + c + 1];
+            const cplx<double> u0 = mk((double)u0f.re, (double)u0f.im), u1 = mk((double)u1f.re, (double)u1f.im);
+            fma_c(a00, h0, u0);
+            fma_c(a01, h0, u1);
+            fma_c(a10, h1, u0);
+            fma_c(a11, h1, u1);
         }
-        __syncthreads();
-        for (int e = tid; e < NN; e += nt) {
-            int i = e / N, n = e % N;
-            cplx<double> acc = Us[e];
-            for (int m = 0; m < N; ++m) fma_c(acc, Us[i * N + m], Ts[m * N + n]);
-            Hs[e] = acc;
-        }
-        __syncthreads();
-        for (int e = tid; e < NN; e += nt) Us[e] = Hs[e];
+        const double l0 = ls[c], l1 = ls[c + 1];
+        auto res = [&](cplx<double> acc, int r, int col, double lv) {
+            const cplx<float> u = Us[r * Np + col];
+            Rs[r * Np + col] = mk((float)(acc.re - lv * (double)u.re), (float)(acc.im - lv * (double)u.im));
+        };
+        res(a00, i, c, l0);
+        res(a01, i, c + 1, l1);
+        res(a10, i + 1, c, l0);
+        res(a11, i + 1, c + 1, l1);
     }
+    __syncthreads();
+    // P = U^dag R (FP32)
+    smem_cgemm<float, true>(Np, Np, Us, Rs, Ps, tid, nt);
+    for (int n = tid; n < N; n += nt) {
+        double s = 0.0;
+        for (int l = 0; l < N; ++l) {
+            const cplx<float> u = Us[l * Np + n];
+            s += (double)u.re * u.re + (double)u.im * u.im;
+        }
+        Sn[n] = s;
+    }
+    __syncthreads();
+    for (int n = tid; n < N; n += nt) rho[n] = (double)ls[n] + (double)Ps[n * Np + n].re / Sn[n];
     __syncthreads();
     for (int n = tid; n < N; n += nt) {
-        const double en = Ev[n];
-        int rank = 0;
-        for (int j = 0; j < N; ++j) rank += (Ev[j] < en || (Ev[j] == en && j < n)) ? 1 : 0;
-        E64[(size_t)k * N + rank] = en;
-        for (int row = 0; row < N; ++row) {
-            const cplx<double> u = Us[row * N + n];
-            U[(size_t)k * NN + row * N + rank] = mk((float)u.re, (float)u.im);
+        double e2 = rho[n];
+        bool bad = !isfinite(e2);
+        for (int m = 0; m < N; ++m) {
+            if (m == n) continue;
+            const double d = rho[n] - rho[m];
+            if (!(fabs(d) > degen_gap)) { bad = true; continue; }
+            const cplx<float> p = Ps[m * Np + n];
+            e2 += ((double)p.re * p.re + (double)p.im * p.im) / d;
         }
-        if (!isfinite(en)) s_flag = 1;
+        En[n] = e2;
+        if (bad || !isfinite(e2)) s_flag = 1;
+    }
+    __syncthreads();
+    // C in place of P (zero diagonal and zero for flagged gaps)
+    for (int e = tid; e < NPP; e += nt) {
+        const int m = e / Np, n = e % Np;
+        cplx<float> c = mk(0.f, 0.f);
+        if (m < N && n < N && m != n) {
+            const double d = rho[n] - rho[m];
+            if (fabs(d) > degen_gap) c = mk((float)((double)Ps[e].re / d), (float)((double)Ps[e].im / d));
+        }
+        Ps[e] = c;
+    }
+    __syncthreads();
+    // U' = U + U C (FP32) into Rs
+    smem_cgemm<float, false>(Np, Np, Us, Ps, Rs, tid, nt);
+    __syncthreads();
+    for (int n = tid; n < N; n += nt) {
+        const double en = En[n];
+        int rank = 0;
+        for (int j = 0; j < N; ++j) rank += (En[j] < en || (En[j] == en && j < n)) ? 1 : 0;
+        E64[(size_t)k * N + rank] = en;
+        const float sc = (float)(1.0 / sqrt(Sn[n]));
+        for (int row = 0; row < N; ++row) {
+            const cplx<float> u = Us[row * Np + n] + Rs[row * Np + n];
+            U[(size_t)k * NN + row * N + rank] = mk(u.re * sc, u.im * sc);
+        }
     }
     __syncthreads();
     if (tid == 0 && redo_flag) redo_flag[k] = s_flag ? 1 : 0;
 }
 
-// Mixed form without the FP64 refinement: flag the k-points whose result
-// could flip under the FP32 eigenvalue error -- a Niu term whose product
-// denominator |(E0-En)^2 (E0-Em)| lies within a relative mask_eps of kuboTol
-// (src/mep_niu.f90:72-73, :131-132), or, for the T = 0 step occupation, a band
-// within fermi_eps of a Fermi energy -- for the FP64 rerun, and hand the FP32
-// energies on as FP64.
-__global__ void __launch_bounds__(128) window_flag_kernel(int N, const float* __restrict__ E32, double* __restrict__ E64,
-                                                          int nval, float tol, float mask_eps, int nE,
-                                                          const double* __restrict__ ef, int step_occ,
-                                                          double fermi_eps, int* __restrict__ flags) {
-    __shared__ float Es[kMaxN];
-    __shared__ int hit;
-    const int64_t k = blockIdx.x;
-    const int tid = threadIdx.x, NN = N * N;
-    if (tid == 0) hit = 0;
-    for (int n = tid; n < N; n += blockDim.x) {
-        const float e = E32[(size_t)k * N + n];
-        Es[n] = e;
-        E64[(size_t)k * N + n] = (double)e;
-    }
-    __syncthreads();
-    int h = 0;
-    if (flags) {
-        const float lo = tol * (1.f - mask_eps), hi = tol * (1.f + mask_eps);
-        for (int t = tid; t < nval * NN; t += blockDim.x) {
-            const int n0 = t / NN, n = (t / N) % N, m = t % N;
-            if (n == n0 || m == n0) continue;
-            const float d0n = Es[n0] - Es[n], d0m = Es[n0] - Es[m];
-            const float den = fabsf(d0n * d0n * d0m);
-            h |= (den >= lo && den <= hi) ? 1 : 0;
-        }
-        if (step_occ)
-            for (int t = tid; t < N * nE; t += blockDim.x) {
-                const int n = t / nE, e = t % nE;
-                h |= (fabs((double)Es[n] - ef[e]) < fermi_eps) ? 1 : 0;
-            }
-        if (h) atomicOr(&hit, 1);
-    }
-    __syncthreads();
-    if (flags && tid == 0 && hit) flags[k] = 1;
+size_t refine_smem_bytes(int N) {
+    const size_t Np = N + (N & 1);
+    return Np * Np * sizeof(cplx<double>) + 3 * Np * sizeof(double) + 3 * Np * Np * sizeof(cplx<float>);
 }
 
-cudaError_t launch_window_flags(int N, int64_t nk, const float* E32, double* E64, int nval, double tol, double mask_eps,
-                                int nE, const double* ef, int step_occ, double fermi_eps, int* flags, cudaStream_t s) {
+cudaError_t launch_refine(int N, int64_t nk, const cplx<double>* H64, const float* lam, cplx<float>* U, double* E64,
+                          double degen_gap, int* redo_flag, cudaStream_t s) {
     if (nk <= 0) return cudaSuccess;
-    window_flag_kernel<<<(unsigned)nk, 128, 0, s>>>(N, E32, E64, nval, (float)tol, (float)mask_eps, nE, ef, step_occ,
-                                                    fermi_eps, flags);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_refine(int N, int64_t nk, const cplx<double>* H64, cplx<float>* U, double* E64, double degen_gap,
-                          int first_order, int* redo_flag, cudaStream_t s) {
-    if (nk <= 0) return cudaSuccess;
-    const size_t smem = 3 * (size_t)N * N * sizeof(cplx<double>) + (size_t)N * sizeof(double);
+    const size_t smem = refine_smem_bytes(N);
     cudaError_t e = cudaFuncSetAttribute(refine_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    refine_kernel<<<(unsigned)nk, N <= 16 ? 128 : 256, smem, s>>>(N, H64, U, E64, degen_gap, first_order, redo_flag);
+    refine_kernel<<<(unsigned)nk, N <= 16 ? 128 : 256, smem, s>>>(N, H64, lam, U, E64, degen_gap, redo_flag);
     return cudaGetLastError();
 }
 

@@ -25,44 +25,6 @@ constexpr int RT = 8;    // R vectors per shared-memory stage
 constexpr int NT = 256;  // threads
 
 template <typename T, int NB>
-__device__ __forceinline__ void ft_epilogue(const DevModel& m, const double k[3], int pair, const cplx<double> (&X)[NB],
-                                            cplx<T>* __restrict__ Wk, int NN) {
-    const int n = pair / m.N, mm = pair % m.N;
-    cplx<double> psi = mk(1.0, 0.0);
-    double dt[3] = {0.0, 0.0, 0.0};
-    if (m.has_tau) {
-        double d[3];
-        for (int i = 0; i < 3; ++i) d[i] = m.tau[mm * 3 + i] - m.tau[n * 3 + i];
-        double x = k[0] * d[0] + k[1] * d[1] + k[2] * d[2];
-        double s, c;
-        sincospi(2.0 * x, &s, &c);
-        psi = mk(c, s);
-        for (int a = 0; a < 3; ++a) dt[a] = m.C[a * 3 + 0] * d[0] + m.C[a * 3 + 1] * d[1] + m.C[a * 3 + 2] * d[2];
-    }
-    cplx<double> H = psi * X[0];
-    Wk[pair] = mk((T)H.re, (T)H.im);
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        cplx<double> v = times_i(psi * X[1 + a] + dt[a] * H);
-        Wk[(size_t)(1 + a) * NN + pair] = mk((T)v.re, (T)v.im);
-    }
-    if constexpr (NB == 10) {
-        cplx<double> A[3];
-#pragma unroll
-        for (int b = 0; b < 3; ++b) {
-            A[b] = psi * X[4 + b];
-            Wk[(size_t)(4 + b) * NN + pair] = mk((T)A[b].re, (T)A[b].im);
-        }
-        const int qa[3] = {0, 0, 1}, qb[3] = {1, 2, 2};
-#pragma unroll
-        for (int q = 0; q < 3; ++q) {
-            cplx<double> v = times_i(psi * X[7 + q] + dt[qa[q]] * A[qb[q]] - dt[qb[q]] * A[qa[q]]);
-            Wk[(size_t)(7 + q) * NN + pair] = mk((T)v.re, (T)v.im);
-        }
-    }
-}
-
-template <typename T, int NB>
 __global__ void __launch_bounds__(NT) ft_simt_kernel(DevModel m, KRange kr, cplx<T>* __restrict__ W) {
     __shared__ cplx<double> Ps[RT][TK];
     __shared__ cplx<double> Ss[RT][TP * NB];

@@ -127,6 +127,53 @@ struct DevModel {
     const double* tau;        // (N, 3) or nullptr
 };
 
+// Tight-binding phase epilogue of the Fourier sums for one (n,m) pair of one
+// k-point: from the raw sums X_b = sum_R exp(2 pi i k.R) S_b(R) it writes the
+// W-gauge blocks, with psi = exp(2 pi i k.(tau_m - tau_n)) and
+// dt = C (tau_m - tau_n):
+//     H = psi X_0,  H_a = i (psi X_a + dt_a H),  A_b = psi X_{3+b},
+//     Om_ab = i (psi X_Q + dt_a A_b - dt_b A_a)
+// (the per-element angle 2 pi k.(R + tau_m - tau_n) of
+// src/wann_interp.f90:192-281 factorised; the Wannier convention is tau = 0).
+template <typename T, int NB>
+__device__ __forceinline__ void ft_epilogue(const DevModel& m, const double k[3], int pair, const cplx<double> (&X)[NB],
+                                            cplx<T>* __restrict__ Wk, int NN) {
+    const int n = pair / m.N, mm = pair % m.N;
+    cplx<double> psi = mk(1.0, 0.0);
+    double dt[3] = {0.0, 0.0, 0.0};
+    if (m.has_tau) {
+        double d[3];
+        for (int i = 0; i < 3; ++i) d[i] = m.tau[mm * 3 + i] - m.tau[n * 3 + i];
+        double x = k[0] * d[0] + k[1] * d[1] + k[2] * d[2];
+        double s, c;
+        sincospi(2.0 * x, &s, &c);
+        psi = mk(c, s);
+        for (int a = 0; a < 3; ++a) dt[a] = m.C[a * 3 + 0] * d[0] + m.C[a * 3 + 1] * d[1] + m.C[a * 3 + 2] * d[2];
+    }
+    cplx<double> H = psi * X[0];
+    Wk[pair] = mk((T)H.re, (T)H.im);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        cplx<double> v = times_i(psi * X[1 + a] + dt[a] * H);
+        Wk[(size_t)(1 + a) * NN + pair] = mk((T)v.re, (T)v.im);
+    }
+    if constexpr (NB == 10) {
+        cplx<double> A[3];
+#pragma unroll
+        for (int b = 0; b < 3; ++b) {
+            A[b] = psi * X[4 + b];
+            Wk[(size_t)(4 + b) * NN + pair] = mk((T)A[b].re, (T)A[b].im);
+        }
+        const int qa[3] = {0, 0, 1}, qb[3] = {1, 2, 2};
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            cplx<double> v = times_i(psi * X[7 + q] + dt[qa[q]] * A[qb[q]] - dt[qb[q]] * A[qa[q]]);
+            Wk[(size_t)(7 + q) * NN + pair] = mk((T)v.re, (T)v.im);
+        }
+    }
+}
+
+
 struct JobDev {
     int nE, nval, do_ahc, do_mep, do_kubo;
     double T_kelvin;
@@ -155,10 +202,8 @@ cudaError_t launch_eig(int N, int64_t nk, const cplx<T>* W, int nbW, const cplx<
                        int max_sweeps, int* sweeps_max, int* flag_cap, double degen_gap, int* redo_flag,
                        cudaStream_t s);
 cudaError_t launch_ft_h64(const DevModel& m, const KRange& kr, cplx<double>* H64, cudaStream_t s);
-cudaError_t launch_refine(int N, int64_t nk, const cplx<double>* H64, cplx<float>* U, double* E64, double degen_gap,
-                          int first_order, int* redo_flag, cudaStream_t s);
-cudaError_t launch_window_flags(int N, int64_t nk, const float* E32, double* E64, int nval, double tol, double mask_eps,
-                                int nE, const double* ef, int step_occ, double fermi_eps, int* flags, cudaStream_t s);
+cudaError_t launch_refine(int N, int64_t nk, const cplx<double>* H64, const float* lam, cplx<float>* U, double* E64,
+                          double degen_gap, int* redo_flag, cudaStream_t s);
 template <typename T>
 cudaError_t launch_rot(const DevModel& m, int64_t nk, const cplx<T>* W, const cplx<T>* U, cplx<T>* HA,
                        cplx<T>* OD, cudaStream_t s);
@@ -169,6 +214,28 @@ template <typename T>
 cudaError_t launch_bandsum(const DevModel& m, const JobDev& j, int64_t nk, const double* E, const cplx<T>* V,
                            const T* CSV, const int* skip, double* partials, int n_cta, cudaStream_t s);
 cudaError_t launch_reduce(const double* partials, int n_cta, int size, double* out, cudaStream_t s);
+
+// Separable Fourier sums on a Monkhorst-Pack mesh (ft_sep.cu).  The slabs
+// G2[qx][qy][iz][blk][pair] stay resident in HBM for the run.
+struct SepPlan {
+    bool ready = false;
+    bool fp64 = false;              // G2d holds all blocks (FP64 form); else G2f all + G2d block 0
+    int N = 0, nbk = 0, nbd = 0;    // n_wf, stack blocks, blocks in G2d
+    int mp[3] = {0, 0, 0}, lo[3] = {0, 0, 0}, nb[3] = {0, 0, 0};  // mesh, R box origin and size
+    cplx<double>* G2d = nullptr;
+    cplx<float>* G2f = nullptr;
+    const double* tau = nullptr;
+    size_t h2d_bytes = 0;
+};
+// 0: plan ready; 1: the model or mesh has no separable form here (non-integer
+// R, an R box wider than 32, or slabs larger than half the free memory);
+// 2/3: CUDA error / out of memory (the MEPI_ERR_* values).
+int sep_plan_build(SepPlan& p, const DevModel& m, const double* R_host, const cplx<double>* S_host, const int mp[3],
+                   bool fp64, cudaStream_t s);
+void sep_plan_free(SepPlan& p);
+cudaError_t launch_sep_h64(const SepPlan& p, const KRange& kr, cplx<double>* H64, cudaStream_t s);
+template <typename T>
+cudaError_t launch_sep_w(const SepPlan& p, const DevModel& m, const KRange& kr, cplx<T>* W, cudaStream_t s);
 int bandsum_ctas();
 
 }  // namespace mepi
