@@ -6,8 +6,10 @@ Workload (one "step" = one pass of the k-loop over the whole mesh):
   R in {-3..3}^3 (nR = 343), hopping decay exp(-|R|/1.5), r(R) present,
   tight-binding phase convention, 128^3 Monkhorst-Pack mesh (2,097,152 k),
   E_F = 0, T = 0, valence_bands = 16; AHC + Niu MEP + Kubo MEP outputs.
-  Default form: mixed (split-FP16 tensor-core Fourier sums, FP32 per-k work,
-  FP64 k-sums and FP64 rerun of near-degenerate k-points).
+  Default form: mixed (separable Fourier sums from FP32 slabs plus FP64 H(k),
+  FP32 Jacobi with an FP64 residual refinement of the eigenpairs, FP32
+  rotation / velocity / band sums with FP64 energies, FP64 k-sums, and an FP64
+  rerun of near-degenerate k-points).
 
 Arms:
   (default)         the CUDA library through its C ABI; `value` times
@@ -133,18 +135,33 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def flops_per_k(N, nR, nval, nE, has_r=True):
-    """Algorithmic real flops per k-point by stage (complex MAC = 8 flops)."""
+def sep_box_z(model):
+    """Extent of the integer R box along z (the per-k length of the separable sums)."""
+    import numpy as np
+    Rz = np.rint(np.asarray(model.R_frac, dtype=np.float64)[:, 2])
+    return int(Rz.max() - Rz.min() + 1)
+
+
+def work_per_k(N, nR, nval, nE, nbz, mixed, column_len, has_r=True):
+    """Algorithmic real flops and HBM bytes per k-point by stage (complex MAC = 8 flops).
+
+    ft: the separable per-k sums (nbz terms per element of every stack block):
+    the W-gauge output (the mixed form does not write its FP32 H block) plus
+    the G2 slab of the k-point's (qx, qy) column shared by the column_len
+    k-points of that column; fth: the FP64 H(k) sums; refine: the compensated
+    residual product and three FP32 products; eig: (80/3) N^3 by convention."""
     nb = 10 if has_r else 4
     r = 1 if has_r else 0
+    c = 8 if mixed else 16          # bytes of one complex element of the per-k work
+    w_blocks = nb - 1 if mixed else nb
     return {
-        "ft": 8.0 * nR * nb * N * N,
-        "fth": 8.0 * nR * N * N,
-        "refine": 3 * 8.0 * N ** 3,
-        "eig": 80.0 / 3.0 * N ** 3,
-        "rot": 16.0 * N ** 3 * (3 + 3 * r) + 24.0 * N ** 3 * r,
-        "gauge": 180.0 * N * N,
-        "bandsum": 48.0 * N ** 3 + 48.0 * N * N * nval + 2.0 * 9 * N * (N + nE) * 4,
+        "ft": (8.0 * nbz * nb * N * N, c * w_blocks * N * N + c * nbz * nb * N * N / column_len),
+        "fth": (8.0 * nbz * N * N, 16.0 * N * N + 16.0 * nbz * N * N / column_len),
+        "refine": (4 * 8.0 * N ** 3, 16.0 * N * N + 2 * 8.0 * N * N + 8.0 * N),
+        "eig": (80.0 / 3.0 * N ** 3, 16.0 * N * N + c * N * N),
+        "rot": (16.0 * N ** 3 * (3 + 3 * r) + 24.0 * N ** 3 * r, c * (nb - 1 + 1) * N * N + c * 6 * N * N),
+        "gauge": (180.0 * N * N, c * 6 * N * N + c * 3 * N * N),
+        "bandsum": (48.0 * N ** 3 + 48.0 * N * N * nval + 2.0 * 9 * N * (N + nE) * 4, c * 3 * N * N + 8.0 * N),
     }
 
 
@@ -220,8 +237,11 @@ def run_gpu(args, rank, world):
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2 (129 MB)
 
     ctx = api.Context(model)
-    for _ in range(max(args.warmup, 3)):
+    plan_ms = None
+    for w in range(max(args.warmup, 3)):
         ctx.core_worker_loc(job, precision=prec, k_stride=ks)
+        if w == 0:
+            plan_ms = ctx.timing()["plan_ms"]   # slab build of the first run on this mesh
     # timed region: exactly K steps, L2 flushed before each one
     clocks = ClockSampler()
     barrier(world)
@@ -266,8 +286,10 @@ def run_gpu(args, rank, world):
         e2e_s = allreduce_max(statistics.median(e2e_times), world)
         e2e_value = world * nk / e2e_s
 
-    # roofline of the dominant kernel (algorithmic flops / average launch time)
-    f = flops_per_k(model.n_wf, model.n_R, job["valence_bands"], len(job["ef_lst"]), model.r is not None)
+    # roofline of the dominant kernel (algorithmic work / average launch time)
+    mixed = prec == api.PREC_MIXED
+    f = work_per_k(model.n_wf, model.n_R, job["valence_bands"], len(job["ef_lst"]), sep_box_z(model), mixed,
+                   max(1, mp[2] // ks), model.r is not None)
     stage_ms = {k: v[0] for k, v in stage.items()}
     dom = max(("ft", "fth", "eig", "refine", "rot", "gauge", "bandsum"), key=lambda k: stage_ms.get(k, 0.0))
     peaks = {}
@@ -275,21 +297,30 @@ def run_gpu(args, rank, world):
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
     except (OSError, ValueError):
         pass
-    flops_per_launch = f[dom] * nk * args.steps / max(stage[dom][1], 1)
-    avg_launch_s = stage_ms[dom] * 1e-3 / max(stage[dom][1], 1)
-    achieved = flops_per_launch / avg_launch_s / 1e12
-    if dom == "ft" and prec == api.PREC_MIXED:
-        bound, peak = "tensor", peaks.get("bf16_tflops", 1900.0)
-        peak_src = "of measured" if "bf16_tflops" in peaks else "of fallback"
+    n_launch = max(stage[dom][1], 1)
+    flops_per_launch = f[dom][0] * nk * args.steps / n_launch
+    bytes_per_launch = f[dom][1] * nk * args.steps / n_launch
+    avg_launch_s = stage_ms[dom] * 1e-3 / n_launch
+    if dom == "ft":
+        # the separable sums stream their W-gauge output: an HBM-bound kernel
+        hbm = peaks.get("hbm_gbs", 6800.0)
+        achieved = bytes_per_launch / avg_launch_s / 1e9
+        roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                    "frac": achieved / hbm, "peak_source": "of measured" if "hbm_gbs" in peaks else "of fallback"}
     else:
-        # CUDA-core kernels: FP32 (mixed) / FP64 (plain) FMA pipes
-        bound = "tensor"
-        peak = peaks.get("bf16_tflops", 1900.0)
-        peak_src = "of measured bf16 tensor peak (this kernel runs on CUDA cores)"
-    roofline = {"bound": bound, "kernel": dom, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                "frac": achieved / peak, "peak_source": peak_src, "traffic": None,
-                "flops_per_launch": flops_per_launch, "avg_launch_ms": avg_launch_s * 1e3,
-                "stage_ms_per_step": {k: v / args.steps for k, v in stage_ms.items()}}
+        tensor = peaks.get("bf16_tflops", 1900.0)
+        achieved = flops_per_launch / avg_launch_s / 1e12
+        roofline = {"bound": "tensor", "kernel": dom, "achieved": achieved, "peak": tensor, "unit": "TFLOP/s",
+                    "frac": achieved / tensor,
+                    "peak_source": ("of measured" if "bf16_tflops" in peaks else "of fallback")
+                    + " bf16 tensor peak; this kernel runs on the CUDA cores"}
+        # the pipe it does run on: FP32 (mixed) or FP64 FMA, peaks measured with an FMA probe on a GB300
+        pipe, pipe_peak = ("fp32", 68.0) if mixed and dom != "fth" else ("fp64", 1.19)
+        roofline["cuda_core"] = {"pipe": pipe, "peak_tflops": pipe_peak, "frac": achieved / pipe_peak,
+                                 "peak_source": "FMA-chain probe on a GB300 of this pool"}
+    roofline.update({"traffic": None, "flops_per_launch": flops_per_launch, "bytes_per_launch": bytes_per_launch,
+                     "avg_launch_ms": avg_launch_s * 1e3,
+                     "stage_ms_per_step": {k: v / args.steps for k, v in stage_ms.items()}})
 
     # error of this form against the FP64 path on a strided subset
     err = None
@@ -322,7 +353,7 @@ def run_gpu(args, rank, world):
         out = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": max(args.warmup, 3), "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f16x3 (f64 k-sums)" if prec == api.PREC_MIXED else "f64",
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (f64 H(k), eigen-residual, energies, k-sums)" if prec == api.PREC_MIXED else "f64",
             "data": "synthetic (seeded random tight-binding model)",
             "config": {"workload": args.workload, "n_wf": model.n_wf, "n_R": model.n_R, "mesh": list(mp),
                        "k_points_per_step": nk, "k_stride": ks, "valence_bands": job["valence_bands"], "n_eF": len(job["ef_lst"]),
@@ -330,6 +361,7 @@ def run_gpu(args, rank, world):
                        "parallelism": f"replicas x{world}"},
             "host_ms_per_step": 1e3 * t_host / args.steps,
             "fp64_reruns_per_step": res["n_k_fp64"] if res else None,
+            "plan_ms": plan_ms,
             "clocks": clk,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                     "seconds_per_step": e2e_s},

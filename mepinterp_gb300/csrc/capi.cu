@@ -168,7 +168,7 @@ int run_chunk(mepi_ctx* ctx, const KRange& kr, const JobDev* jb, int n_cta, doub
     int* counters = ctx->counters.as<int>();
     const bool mixed = sizeof(T) == 4;
     int* flags = want_flags ? ctx->flags.as<int>() : nullptr;
-    const bool sep = ctx->sep_active && !kr.kpts && (mixed || ctx->sep.fp64);
+    const bool sep = ctx->sep_active && !kr.kpts && (mixed || ctx->sep.nbd == ctx->sep.nbk);
     if (sep) {
         STAGE(ST_FT, (launch_sep_w<T>(ctx->sep, ctx->dm, kr, ctx->W.as<cplx<T>>(), ctx->stream)));
     } else if (mixed && ctx->ft_pref != 2) {

@@ -31,104 +31,121 @@ template <typename T> struct EigTol;
 template <> struct EigTol<double> { static constexpr double eps = 2.220446049250313e-16, skip = 1e-20; };
 template <> struct EigTol<float> { static constexpr double eps = 1.1920928955078125e-07, skip = 1e-10; };
 
+// Sum over the CTA (256 threads or fewer, a multiple of 32).
 template <typename T>
+__device__ __forceinline__ T cta_sum(T v, T* red) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const int w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) red[w] = v;
+    __syncthreads();
+    T s = 0;
+    for (int i = 0; i < nw; ++i) s += red[i];
+    return s;
+}
+
+// One CTA diagonalises a run of kblock consecutive k-points.  The matrix M
+// and the eigenvector accumulator V live in shared memory as separate real
+// and imaginary planes with row stride NP + 1 (NP = the band count padded to
+// a power of two; padded rows and columns hold zeros in M and the identity
+// in V, and the pairs that touch them are never rotated).  A round of the
+// round-robin ordering rotates NP/2 disjoint pairs at once; because the pairs
+// partition the indices, M <- G^dag M G splits into independent 2 x 2 blocks
+// (rows of pair A, columns of pair B), Z = G_A^dag X G_B, which each thread
+// updates in place -- one pass and two barriers per round.
+template <typename T, int NP>
 __global__ void __launch_bounds__(256) jacobi_kernel(int N, int64_t nk, int kblock, const cplx<T>* __restrict__ W,
                                                      int nbW, const cplx<double>* __restrict__ H64,
                                                      T* __restrict__ E, cplx<T>* __restrict__ U, int max_sweeps,
                                                      int* sweeps_max, int* flag_cap, double degen_gap,
                                                      int* redo_flag) {
+    constexpr int HP = NP / 2, LD = NP + 1, PL = NP * LD;
     extern __shared__ unsigned char smem_raw[];
-    const int ld = N + 1;                       // padded row stride
-    cplx<T>* M = reinterpret_cast<cplx<T>*>(smem_raw);
-    cplx<T>* Vv = M + N * ld;                   // eigenvector accumulator
-    cplx<T>* Ts = Vv + N * ld;                  // warm-start product / sorted copy
-    T* cs = reinterpret_cast<T*>(Ts + N * ld);  // per pair: c, s
-    T* ss = cs + kMaxN / 2;
-    cplx<T>* eph = reinterpret_cast<cplx<T>*>(ss + kMaxN / 2);  // e^{i phi}
-    T* dnew = reinterpret_cast<T*>(eph + kMaxN / 2);           // new diagonal (2 per pair)
-    int* pp = reinterpret_cast<int*>(dnew + kMaxN);
-    int* qq = pp + kMaxN / 2;
-    T* red = reinterpret_cast<T*>(qq + kMaxN / 2);            // reduction scratch [256]
-    __shared__ int s_conv;
-
+    T* Mr = reinterpret_cast<T*>(smem_raw);
+    T* Mi = Mr + PL;
+    T* Vr = Mi + PL;
+    T* Vi = Vr + PL;
+    T* Tr = Vi + PL;  // warm-start product / sorted eigenvectors
+    T* Ti = Tr + PL;
+    __shared__ T s_c[HP], s_s[HP], s_pr[HP], s_pi[HP], s_d0[HP], s_d1[HP];
+    __shared__ int s_p[HP], s_q[HP], s_fix[HP];
+    __shared__ T red[8];
+    __shared__ T s_E[NP];
     const int tid = threadIdx.x, nt = blockDim.x;
     const int NN = N * N;
-    const int Np = N + (N & 1);
-    const int half = Np / 2;
-    const int Np1 = Np - 1;
 
     for (int jb = 0; jb < kblock; ++jb) {
         const int64_t k = (int64_t)blockIdx.x * kblock + jb;
         if (k >= nk) break;
-        const bool warm = jb > 0;   // Vv holds the previous k-point's sorted eigenvectors
+        const bool warm = jb > 0;   // V holds the previous k-point's sorted eigenvectors
         __syncthreads();
         // load (from the FP64 H(k) when given), Hermitise from the upper triangle
-        for (int e = tid; e < NN; e += nt) {
-            int i = e / N, j = e % N;
-            int a = i < j ? i : j, b = i < j ? j : i;
-            cplx<T> h;
-            if (H64) {
-                const cplx<double> x = H64[(size_t)k * NN + a * N + b];
-                h = mk((T)x.re, (T)x.im);
-            } else {
-                h = W[(size_t)k * nbW * NN + a * N + b];
-            }
-            cplx<T> v = (i < j) ? h : (i > j) ? conjg(h) : mk(h.re, (T)0);
-            M[i * ld + j] = v;
-            if (!warm) Vv[i * ld + j] = mk((T)(i == j ? 1 : 0), (T)0);
-        }
-        // ||H||_F^2 (unchanged by the unitary warm start)
         T part = 0;
-        for (int e = tid; e < NN; e += nt) {
-            int i = e / N, j = e % N;
-            part += abs2(M[i * ld + j]);
+        for (int e = tid; e < NP * NP; e += nt) {
+            const int i = e / NP, j = e % NP;
+            cplx<T> v = mk((T)0, (T)0);
+            if (i < N && j < N) {
+                const int a = i < j ? i : j, b = i < j ? j : i;
+                cplx<T> h;
+                if (H64) {
+                    const cplx<double> x = H64[(size_t)k * NN + a * N + b];
+                    h = mk((T)x.re, (T)x.im);
+                } else {
+                    h = W[(size_t)k * nbW * NN + a * N + b];
+                }
+                v = (i < j) ? h : (i > j) ? conjg(h) : mk(h.re, (T)0);
+            }
+            Mr[i * LD + j] = v.re;
+            Mi[i * LD + j] = v.im;
+            part += abs2(v);
+            if (!warm) {
+                Vr[i * LD + j] = (T)(i == j ? 1 : 0);
+                Vi[i * LD + j] = (T)0;
+            }
         }
-        red[tid] = part;
-        __syncthreads();
-        for (int w = nt / 2; w > 0; w >>= 1) {
-            if (tid < w) red[tid] += red[tid + w];
-            __syncthreads();
-        }
-        const T fro2 = red[0];
-        __syncthreads();
+        const T fro2 = cta_sum(part, red);   // ||H||_F^2, unchanged by the unitary warm start
         if (warm) {
-            // M <- V^dag H V with V the previous eigenvectors (neighbouring k)
-            if ((N & 1) == 0) {
-                smem_cgemm<T, false>(N, ld, M, Vv, Ts, tid, nt);
-                __syncthreads();
-                smem_cgemm<T, true>(N, ld, Vv, Ts, M, tid, nt);
-            } else {
-                for (int e = tid; e < NN; e += nt) {
-                    int i = e / N, c = e % N;
-                    cplx<T> acc = mk((T)0, (T)0);
-                    for (int l = 0; l < N; ++l) fma_c(acc, M[i * ld + l], Vv[l * ld + c]);
-                    Ts[i * ld + c] = acc;
+            // T = M V, then M = V^dag T (2 x 2 output tiles per thread)
+            for (int t = tid; t < HP * HP; t += nt) {
+                const int i = 2 * (t / HP), j = 2 * (t % HP);
+                cplx<T> c00 = mk((T)0, (T)0), c01 = c00, c10 = c00, c11 = c00;
+                for (int l = 0; l < NP; ++l) {
+                    const cplx<T> a0 = mk(Mr[i * LD + l], Mi[i * LD + l]), a1 = mk(Mr[(i + 1) * LD + l], Mi[(i + 1) * LD + l]);
+                    const cplx<T> b0 = mk(Vr[l * LD + j], Vi[l * LD + j]), b1 = mk(Vr[l * LD + j + 1], Vi[l * LD + j + 1]);
+                    fma_c(c00, a0, b0); fma_c(c01, a0, b1); fma_c(c10, a1, b0); fma_c(c11, a1, b1);
                 }
-                __syncthreads();
-                for (int e = tid; e < NN; e += nt) {
-                    int i = e / N, c = e % N;
-                    cplx<T> acc = mk((T)0, (T)0);
-                    for (int l = 0; l < N; ++l) fma_cjc(acc, Vv[l * ld + i], Ts[l * ld + c]);
-                    M[i * ld + c] = acc;
+                Tr[i * LD + j] = c00.re; Ti[i * LD + j] = c00.im;
+                Tr[i * LD + j + 1] = c01.re; Ti[i * LD + j + 1] = c01.im;
+                Tr[(i + 1) * LD + j] = c10.re; Ti[(i + 1) * LD + j] = c10.im;
+                Tr[(i + 1) * LD + j + 1] = c11.re; Ti[(i + 1) * LD + j + 1] = c11.im;
+            }
+            __syncthreads();
+            for (int t = tid; t < HP * HP; t += nt) {
+                const int i = 2 * (t / HP), j = 2 * (t % HP);
+                cplx<T> c00 = mk((T)0, (T)0), c01 = c00, c10 = c00, c11 = c00;
+                for (int l = 0; l < NP; ++l) {
+                    const cplx<T> a0 = conjg(mk(Vr[l * LD + i], Vi[l * LD + i]));
+                    const cplx<T> a1 = conjg(mk(Vr[l * LD + i + 1], Vi[l * LD + i + 1]));
+                    const cplx<T> b0 = mk(Tr[l * LD + j], Ti[l * LD + j]), b1 = mk(Tr[l * LD + j + 1], Ti[l * LD + j + 1]);
+                    fma_c(c00, a0, b0); fma_c(c01, a0, b1); fma_c(c10, a1, b0); fma_c(c11, a1, b1);
                 }
+                Mr[i * LD + j] = c00.re; Mi[i * LD + j] = c00.im;
+                Mr[i * LD + j + 1] = c01.re; Mi[i * LD + j + 1] = c01.im;
+                Mr[(i + 1) * LD + j] = c10.re; Mi[(i + 1) * LD + j] = c10.im;
+                Mr[(i + 1) * LD + j + 1] = c11.re; Mi[(i + 1) * LD + j + 1] = c11.im;
             }
             __syncthreads();
             // restore exact Hermiticity of the rotated matrix
-            for (int e = tid; e < NN; e += nt) {
-                int i = e / N, j = e % N;
+            for (int e = tid; e < NP * NP; e += nt) {
+                const int i = e / NP, j = e % NP;
                 if (i < j) {
-                    cplx<T> x = M[i * ld + j], y = M[j * ld + i];
-                    cplx<T> h = mk((T)0.5 * (x.re + y.re), (T)0.5 * (x.im - y.im));
-                    Ts[i * ld + j] = h;
-                    Ts[j * ld + i] = conjg(h);
+                    const T re = (T)0.5 * (Mr[i * LD + j] + Mr[j * LD + i]);
+                    const T im = (T)0.5 * (Mi[i * LD + j] - Mi[j * LD + i]);
+                    Mr[i * LD + j] = re; Mi[i * LD + j] = im;
+                    Mr[j * LD + i] = re; Mi[j * LD + i] = -im;
                 } else if (i == j) {
-                    Ts[i * ld + i] = mk(M[i * ld + i].re, (T)0);
+                    Mi[i * LD + i] = (T)0;
                 }
-            }
-            __syncthreads();
-            for (int e = tid; e < NN; e += nt) {
-                int i = e / N, j = e % N;
-                M[i * ld + j] = Ts[i * ld + j];
             }
             __syncthreads();
         }
@@ -136,154 +153,119 @@ __global__ void __launch_bounds__(256) jacobi_kernel(int N, int64_t nk, int kblo
         const T tolr = (T)(4.0 * EigTol<T>::eps) * sqrt((T)N);
         const T tol2 = tolr * tolr * fro2;
         const T gskip = (T)EigTol<T>::skip * sqrt(fro2);
+        auto off_norm = [&]() {
+            T o = 0;
+            for (int e = tid; e < NP * NP; e += nt) {
+                const int i = e / NP, j = e % NP;
+                if (i != j) o += Mr[i * LD + j] * Mr[i * LD + j] + Mi[i * LD + j] * Mi[i * LD + j];
+            }
+            return cta_sum(o, red);
+        };
         int sweep = 0;
-        bool converged = (N == 1);
         // a warm start may already be converged: test before the first sweep
-        if (warm) {
-            T off = 0;
-            for (int e = tid; e < NN; e += nt) {
-                int i = e / N, j = e % N;
-                if (i != j) off += abs2(M[i * ld + j]);
-            }
-            red[tid] = off;
-            __syncthreads();
-            for (int w = nt / 2; w > 0; w >>= 1) {
-                if (tid < w) red[tid] += red[tid + w];
-                __syncthreads();
-            }
-            if (tid == 0) s_conv = (red[0] <= tol2) ? 1 : 0;
-            __syncthreads();
-            converged = s_conv != 0;
-            __syncthreads();
-        }
+        bool converged = (N == 1) || (warm && off_norm() <= tol2);
         for (sweep = 0; sweep < max_sweeps && !converged; ++sweep) {
-            for (int r = 0; r < Np1; ++r) {
-                // 1. rotation parameters for the pairs of this round
-                if (tid < half) {
-                    int a, b;
-                    if (tid == 0) { a = Np1; b = r; }
-                    else { a = (r + tid) % Np1; b = (r - tid + Np1) % Np1; }
-                    int p = a < b ? a : b, q = a < b ? b : a;
-                    T c = 1, s = 0;
-                    cplx<T> ph = mk((T)1, (T)0);
+            for (int r = 0; r < NP - 1; ++r) {
+                // 1. rotation parameters of the pairs of this round
+                if (tid < HP) {
+                    const int a = tid == 0 ? NP - 1 : (r + tid) % (NP - 1);
+                    const int b = tid == 0 ? r : (r - tid + NP - 1) % (NP - 1);
+                    const int p = a < b ? a : b, q = a < b ? b : a;
+                    T c = 1, sn = 0, pr = 1, pi = 0, d0 = 0, d1 = 0;
+                    int fix = 0;
                     if (q < N) {
-                        T app = M[p * ld + p].re, aqq = M[q * ld + q].re;
-                        cplx<T> apq = M[p * ld + q];
-                        T g = sqrt(abs2(apq));
+                        const T app = Mr[p * LD + p], aqq = Mr[q * LD + q];
+                        const T xr = Mr[p * LD + q], xi = Mi[p * LD + q];
+                        const T g = sqrt(xr * xr + xi * xi);
                         if (g > gskip) {
-                            T theta = (aqq - app) / (2 * g);
-                            T t = (theta >= 0 ? (T)1 : (T)-1) / (fabs(theta) + sqrt((T)1 + theta * theta));
+                            const T theta = (aqq - app) / (2 * g);
+                            const T t = (theta >= 0 ? (T)1 : (T)-1) / (fabs(theta) + sqrt((T)1 + theta * theta));
                             c = (T)1 / sqrt((T)1 + t * t);
-                            s = t * c;
-                            ph = mk(apq.re / g, apq.im / g);
-                            dnew[2 * tid] = app - t * g;
-                            dnew[2 * tid + 1] = aqq + t * g;
-                        } else {
-                            dnew[2 * tid] = app;
-                            dnew[2 * tid + 1] = aqq;
+                            sn = t * c;
+                            pr = xr / g;
+                            pi = xi / g;
+                            d0 = app - t * g;
+                            d1 = aqq + t * g;
+                            fix = 1;
                         }
-                    } else {
-                        p = q = -1;
                     }
-                    pp[tid] = p; qq[tid] = q; cs[tid] = c; ss[tid] = s; eph[tid] = ph;
+                    s_p[tid] = p; s_q[tid] = q; s_c[tid] = c; s_s[tid] = sn; s_pr[tid] = pr; s_pi[tid] = pi;
+                    s_d0[tid] = d0; s_d1[tid] = d1; s_fix[tid] = fix;
                 }
                 __syncthreads();
-                // 2. column pass M <- M G and U <- U G (consecutive threads walk the
-                //    rows of one pair: padded rows put them in distinct banks)
-                for (int e = tid; e < N * half; e += nt) {
-                    int j = e / N, i = e % N;
-                    int p = pp[j], q = qq[j];
-                    if (p < 0) continue;
-                    T c = cs[j], s = ss[j];
-                    cplx<T> ph = eph[j];
-                    cplx<T> xp = M[i * ld + p], xq = M[i * ld + q];
-                    // X'[i][p] = c xp - s e^{-i phi} xq ; X'[i][q] = s e^{i phi} xp + c xq
-                    M[i * ld + p] = c * xp - s * mul_cj(xq, ph);
-                    M[i * ld + q] = s * (ph * xp) + c * xq;
-                    cplx<T> vp = Vv[i * ld + p], vq = Vv[i * ld + q];
-                    Vv[i * ld + p] = c * vp - s * mul_cj(vq, ph);
-                    Vv[i * ld + q] = s * (ph * vp) + c * vq;
-                }
-                __syncthreads();
-                // 3. row pass M <- G^dag M (consecutive threads walk one row)
-                for (int e = tid; e < N * half; e += nt) {
-                    int j = e / N, i = e % N;
-                    int p = pp[j], q = qq[j];
-                    if (p < 0) continue;
-                    T c = cs[j], s = ss[j];
-                    cplx<T> ph = eph[j];
-                    cplx<T> xp = M[p * ld + i], xq = M[q * ld + i];
-                    // X'[p][i] = c xp - s e^{i phi} xq ; X'[q][i] = s e^{-i phi} xp + c xq
-                    M[p * ld + i] = c * xp - s * (ph * xq);
-                    M[q * ld + i] = s * mul_cj(xp, ph) + c * xq;
-                }
-                __syncthreads();
-                // 4. exact 2x2 result on the rotated pairs
-                if (tid < half) {
-                    int p = pp[tid], q = qq[tid];
-                    if (p >= 0) {
-                        M[p * ld + p] = mk(dnew[2 * tid], (T)0);
-                        M[q * ld + q] = mk(dnew[2 * tid + 1], (T)0);
-                        M[p * ld + q] = mk((T)0, (T)0);
-                        M[q * ld + p] = mk((T)0, (T)0);
+                // 2. M <- G^dag M G, one 2 x 2 block per (pair A, pair B)
+                for (int t = tid; t < HP * HP; t += nt) {
+                    const int A = t / HP, B = t % HP;
+                    const int pA = s_p[A], qA = s_q[A], pB = s_p[B], qB = s_q[B];
+                    const T cA = s_c[A], sA = s_s[A], cB = s_c[B], sB = s_s[B];
+                    const cplx<T> phA = mk(s_pr[A], s_pi[A]), phB = mk(s_pr[B], s_pi[B]);
+                    const cplx<T> x00 = mk(Mr[pA * LD + pB], Mi[pA * LD + pB]), x01 = mk(Mr[pA * LD + qB], Mi[pA * LD + qB]);
+                    const cplx<T> x10 = mk(Mr[qA * LD + pB], Mi[qA * LD + pB]), x11 = mk(Mr[qA * LD + qB], Mi[qA * LD + qB]);
+                    // Y = X G_B: column p' = c xp - s e^{-i phi} xq ; column q' = s e^{i phi} xp + c xq
+                    const cplx<T> y00 = cB * x00 - sB * mul_cj(x01, phB), y01 = sB * (phB * x00) + cB * x01;
+                    const cplx<T> y10 = cB * x10 - sB * mul_cj(x11, phB), y11 = sB * (phB * x10) + cB * x11;
+                    // Z = G_A^dag Y: row p' = c yp - s e^{i phi} yq ; row q' = s e^{-i phi} yp + c yq
+                    cplx<T> z00 = cA * y00 - sA * (phA * y10), z01 = cA * y01 - sA * (phA * y11);
+                    cplx<T> z10 = sA * mul_cj(y00, phA) + cA * y10, z11 = sA * mul_cj(y01, phA) + cA * y11;
+                    if (A == B && s_fix[A]) {
+                        // exact 2 x 2 result on the rotated pair
+                        z00 = mk(s_d0[A], (T)0);
+                        z11 = mk(s_d1[A], (T)0);
+                        z01 = z10 = mk((T)0, (T)0);
                     }
+                    Mr[pA * LD + pB] = z00.re; Mi[pA * LD + pB] = z00.im;
+                    Mr[pA * LD + qB] = z01.re; Mi[pA * LD + qB] = z01.im;
+                    Mr[qA * LD + pB] = z10.re; Mi[qA * LD + pB] = z10.im;
+                    Mr[qA * LD + qB] = z11.re; Mi[qA * LD + qB] = z11.im;
+                }
+                // 3. V <- V G (consecutive threads walk the rows of one pair)
+                for (int t = tid; t < NP * HP; t += nt) {
+                    const int j = t / NP, i = t % NP;
+                    const int p = s_p[j], q = s_q[j];
+                    const T c = s_c[j], sn = s_s[j];
+                    const cplx<T> ph = mk(s_pr[j], s_pi[j]);
+                    const cplx<T> vp = mk(Vr[i * LD + p], Vi[i * LD + p]), vq = mk(Vr[i * LD + q], Vi[i * LD + q]);
+                    const cplx<T> np_ = c * vp - sn * mul_cj(vq, ph), nq = sn * (ph * vp) + c * vq;
+                    Vr[i * LD + p] = np_.re; Vi[i * LD + p] = np_.im;
+                    Vr[i * LD + q] = nq.re; Vi[i * LD + q] = nq.im;
                 }
                 __syncthreads();
             }
-            // convergence: off-diagonal norm
-            T off = 0;
-            for (int e = tid; e < NN; e += nt) {
-                int i = e / N, j = e % N;
-                if (i != j) off += abs2(M[i * ld + j]);
-            }
-            red[tid] = off;
-            __syncthreads();
-            for (int w = nt / 2; w > 0; w >>= 1) {
-                if (tid < w) red[tid] += red[tid + w];
-                __syncthreads();
-            }
-            if (tid == 0) s_conv = (red[0] <= tol2) ? 1 : 0;
-            __syncthreads();
-            converged = s_conv != 0;
-            __syncthreads();
+            converged = off_norm() <= tol2;
         }
         if (tid == 0) {
             atomicMax(sweeps_max, sweep);
             if (!converged) atomicAdd(flag_cap, 1);
         }
         // sort ascending (stable on ties), write E and U, keep the sorted
-        // eigenvectors in Vv as the next k-point's warm start
-        T* dg = red;  // reuse: diagonal values
-        for (int i = tid; i < N; i += nt) dg[i] = M[i * ld + i].re;
-        __syncthreads();
+        // eigenvectors as the next k-point's warm start
         for (int i = tid; i < N; i += nt) {
-            T ei = dg[i];
+            const T ei = Mr[i * LD + i];
             int rank = 0;
             for (int j = 0; j < N; ++j) {
-                T ej = dg[j];
+                const T ej = Mr[j * LD + j];
                 rank += (ej < ei || (ej == ei && j < i)) ? 1 : 0;
             }
+            s_E[rank] = ei;
             E[(size_t)k * N + rank] = ei;
             for (int row = 0; row < N; ++row) {
-                const cplx<T> v = Vv[row * ld + i];
-                U[(size_t)k * NN + row * N + rank] = v;
-                Ts[row * ld + rank] = v;
+                const T vr = Vr[row * LD + i], vi = Vi[row * LD + i];
+                U[(size_t)k * NN + row * N + rank] = mk(vr, vi);
+                Tr[row * LD + rank] = vr;
+                Ti[row * LD + rank] = vi;
             }
         }
         __syncthreads();
         if (redo_flag && tid == 0) {
-            // smallest gap between any two eigenvalues
+            // smallest gap between neighbouring sorted eigenvalues
             T mingap = (T)1e30;
-            for (int i = 0; i < N; ++i)
-                for (int j = i + 1; j < N; ++j) {
-                    T d = fabs(dg[i] - dg[j]);
-                    mingap = d < mingap ? d : mingap;
-                }
+            for (int i = 0; i + 1 < N; ++i) mingap = fmin(mingap, s_E[i + 1] - s_E[i]);
             redo_flag[k] = (!converged || (double)mingap < degen_gap || !(mingap == mingap)) ? 1 : 0;
         }
-        for (int e = tid; e < NN; e += nt) {
-            int i = e / N, j = e % N;
-            Vv[i * ld + j] = Ts[i * ld + j];
+        for (int e = tid; e < N * N; e += nt) {
+            const int i = e / N, j = e % N;
+            Vr[i * LD + j] = Tr[i * LD + j];
+            Vi[i * LD + j] = Ti[i * LD + j];
         }
     }
 }
@@ -291,59 +273,63 @@ __global__ void __launch_bounds__(256) jacobi_kernel(int N, int64_t nk, int kblo
 }  // namespace
 
 template <typename T>
-size_t eig_smem_bytes(int N) {
-    const int ld = N + 1;
-    size_t b = 3 * (size_t)N * ld * sizeof(cplx<T>);
-    b += 2 * (kMaxN / 2) * sizeof(T) + (kMaxN / 2) * sizeof(cplx<T>) + kMaxN * sizeof(T);
-    b += 2 * (kMaxN / 2) * sizeof(int) + 256 * sizeof(T);
-    return (b + 15) & ~(size_t)15;
-}
-
-template <typename T>
 cudaError_t launch_eig(int N, int64_t nk, const cplx<T>* W, int nbW, const cplx<double>* H64, T* E, cplx<T>* U,
                        int max_sweeps, int* sweeps_max, int* flag_cap, double degen_gap, int* redo_flag,
                        cudaStream_t s) {
     if (nk <= 0) return cudaSuccess;
-    size_t smem = eig_smem_bytes<T>(N);
-    cudaError_t e = cudaFuncSetAttribute(jacobi_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    int threads = N <= 16 ? 128 : 256;
     // a run of consecutive k-points per CTA, each warm-started from its
-    // neighbour's eigenvectors (consecutive k are adjacent along kx)
+    // neighbour's eigenvectors (consecutive k-points are mesh neighbours)
     const int kblock = 8;
     const unsigned grid = (unsigned)((nk + kblock - 1) / kblock);
-    jacobi_kernel<T><<<grid, threads, smem, s>>>(N, nk, kblock, W, nbW, H64, E, U, max_sweeps, sweeps_max, flag_cap,
-                                                 degen_gap, redo_flag);
-    return cudaGetLastError();
+    auto go = [&](auto kern, int NP, int threads) {
+        const size_t smem = 6 * (size_t)NP * (NP + 1) * sizeof(T);
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        kern<<<grid, threads, smem, s>>>(N, nk, kblock, W, nbW, H64, E, U, max_sweeps, sweeps_max, flag_cap, degen_gap,
+                                         redo_flag);
+        return cudaGetLastError();
+    };
+    if (N <= 8) return go(jacobi_kernel<T, 8>, 8, 64);
+    if (N <= 16) return go(jacobi_kernel<T, 16>, 16, 128);
+    if (N <= 32) return go(jacobi_kernel<T, 32>, 32, 256);
+    if (N <= 64) return go(jacobi_kernel<T, 64>, 64, 256);
+    return cudaErrorInvalidValue;
 }
 
-// FP64 refinement of the FP32 eigenpairs (U, lambda) against the FP64 H(k),
-// in residual form so that a single product runs in FP64:
-//   R = H U - U diag(lambda)                 FP64 (the only cancelling product)
-//   P = U^dag R                              FP32 (R is small: its rounding is
-//                                            relative to |R|, not to |H|)
-//   rho_n = lambda_n + P_nn / S_nn,  S_nn = |u_n|^2      (normalised Rayleigh
-//                                            quotient, FP64)
-//   E_n = rho_n + sum_{m!=n} |P_mn|^2 / (rho_n - rho_m)  (second order)
-//   C_mn = P_mn / (rho_n - rho_m),  U' = (U + U C) diag(S_nn)^-1/2    (FP32)
-// C fixes both the eigenvector error and the loss of orthogonality of the
-// warm-started FP32 vectors to first order: <u'_m|u'_n> = S_mn + C_mn +
-// conj(C_nm) + O(2nd) = O(2nd).  The energies are then exact to third order
-// in |P| / gap and the vectors to second order, for any gap above degen_gap.
-// A k-point with a gap at or below degen_gap, an unconverged FP32 Jacobi run
-// (flag already set) or non-finite values is flagged for the full FP64 rerun.
-// Eigenpairs are re-sorted by the refined energies.
+// Eigenpair refinement of the FP32 Jacobi result (U, lambda) against the
+// FP64 H(k), in residual form so that a single product needs more than FP32:
+//   R = H U - U diag(lambda)    compensated FP32 (Dot2 with H = H_hi + H_lo),
+//                               the only cancelling product
+//   P = U^dag R                 FP32 (R is small: its rounding is relative to
+//                               |R|, not to |H|)
+//   rho_n = lambda_n + P_nn / S_nn,  S_nn = |u_n|^2   (normalised Rayleigh
+//                               quotient, FP64)
+//   E_n = rho_n + sum_{m!=n} |P_mn|^2 / (rho_n - rho_m)        (second order)
+//   C1_mn = P_mn / (rho_n - rho_m)                              (first order)
+//   C2_mn = (X C1)_mn / (rho_n - rho_m),  C2_nn = -|C1_:n|^2 / 2,
+//           X = P without its diagonal                          (second order)
+//   U' = (U + U (C1 + C2)) diag(S_nn)^-1/2                      (FP32)
+// C1 also restores, to first order, the orthogonality the warm-started FP32
+// vectors lose: <u'_m|u'_n> = S_mn + C1_mn + conj(C1_nm) + O(2nd) = O(2nd).
+// Energies are exact to third order in |P| / gap, vectors to third order in
+// the perturbation and second order in the loss of orthogonality, for every
+// gap above degen_gap.  A k-point with a gap at or below degen_gap, an
+// unconverged FP32 Jacobi run (flag already set) or non-finite values is
+// flagged for the full FP64 rerun.  Eigenpairs are re-sorted by the refined
+// energies.
 __global__ void __launch_bounds__(256) refine_kernel(int N, const cplx<double>* __restrict__ H64,
                                                      const float* __restrict__ lam, cplx<float>* __restrict__ U,
                                                      double* __restrict__ E64, double degen_gap,
                                                      int* __restrict__ redo_flag) {
     extern __shared__ unsigned char smem_raw[];
     const int Np = N + (N & 1), NPP = Np * Np, h = Np / 2;
-    cplx<double>* Hs = reinterpret_cast<cplx<double>*>(smem_raw);
-    double* rho = reinterpret_cast<double*>(Hs + NPP);
+    double* rho = reinterpret_cast<double*>(smem_raw);
     double* En = rho + Np;
     double* Sn = En + Np;
-    cplx<float>* Us = reinterpret_cast<cplx<float>*>(Sn + Np);
+    double* Dn = Sn + Np;
+    cplx<float>* Hh = reinterpret_cast<cplx<float>*>(Dn + Np);
+    cplx<float>* Hl = Hh + NPP;
+    cplx<float>* Us = Hl + NPP;
     cplx<float>* Rs = Us + NPP;
     cplx<float>* Ps = Rs + NPP;
     __shared__ float ls[kMaxN];
@@ -361,45 +347,66 @@ __global__ void __launch_bounds__(256) refine_kernel(int N, const cplx<double>* 
             hv = (i < j) ? x : (i > j) ? conjg(x) : mk(x.re, 0.0);
             uv = U[(size_t)k * NN + i * N + j];
         }
-        Hs[e] = hv;
+        const cplx<float> hh = mk((float)hv.re, (float)hv.im);
+        Hh[e] = hh;
+        Hl[e] = mk((float)(hv.re - (double)hh.re), (float)(hv.im - (double)hh.im));
         Us[e] = uv;
     }
     for (int n = tid; n < Np; n += nt) ls[n] = n < N ? lam[(size_t)k * N + n] : 0.f;
     if (tid == 0) s_flag = redo_flag ? redo_flag[k] : 0;
     __syncthreads();
-    // R = H U - U diag(lambda): FP64 accumulation, 2 x 2 tiles per thread
+    // R = H U - U diag(lambda), 2 x 2 tiles per thread: H_hi U in Dot2, H_lo U in FP32
     for (int t = tid; t < h * h; t += nt) {
         const int i = 2 * (t / h), c = 2 * (t % h);
-        cplx<double> a00 = mk(0.0, 0.0), a01 = a00, a10 = a00, a11 = a00;
+        DF sr[2][2], si[2][2];
+        cplx<float> lo[2][2];
+#pragma unroll
+        for (int x = 0; x < 2; ++x)
+#pragma unroll
+            for (int y = 0; y < 2; ++y) {
+                sr[x][y] = DF{0.f, 0.f};
+                si[x][y] = DF{0.f, 0.f};
+                lo[x][y] = mk(0.f, 0.f);
+            }
         for (int l = 0; l < Np; ++l) {
-            const cplx<double> h0 = Hs[i * Np + l], h1 = Hs[(i + 1) * Np + l];
-            const cplx<float> u0f = Us[l * Np + c], u1f = Us[l * Np + c + 1];
-            const cplx<double> u0 = mk((double)u0f.re, (double)u0f.im), u1 = mk((double)u1f.re, (double)u1f.im);
-            fma_c(a00, h0, u0);
-            fma_c(a01, h0, u1);
-            fma_c(a10, h1, u0);
-            fma_c(a11, h1, u1);
+            const cplx<float> h0 = Hh[i * Np + l], h1 = Hh[(i + 1) * Np + l];
+            const cplx<float> g0 = Hl[i * Np + l], g1 = Hl[(i + 1) * Np + l];
+            const cplx<float> u0 = Us[l * Np + c], u1 = Us[l * Np + c + 1];
+            const cplx<float> hx[2] = {h0, h1}, gx[2] = {g0, g1}, uy[2] = {u0, u1};
+#pragma unroll
+            for (int x = 0; x < 2; ++x)
+#pragma unroll
+                for (int y = 0; y < 2; ++y) {
+                    df_add_prod(sr[x][y], hx[x].re, uy[y].re);
+                    df_add_prod(sr[x][y], -hx[x].im, uy[y].im);
+                    df_add_prod(si[x][y], hx[x].re, uy[y].im);
+                    df_add_prod(si[x][y], hx[x].im, uy[y].re);
+                    fma_c(lo[x][y], gx[x], uy[y]);
+                }
         }
-        const double l0 = ls[c], l1 = ls[c + 1];
-        auto res = [&](cplx<double> acc, int r, int col, double lv) {
-            const cplx<float> u = Us[r * Np + col];
-            Rs[r * Np + col] = mk((float)(acc.re - lv * (double)u.re), (float)(acc.im - lv * (double)u.im));
-        };
-        res(a00, i, c, l0);
-        res(a01, i, c + 1, l1);
-        res(a10, i + 1, c, l0);
-        res(a11, i + 1, c + 1, l1);
+#pragma unroll
+        for (int x = 0; x < 2; ++x)
+#pragma unroll
+            for (int y = 0; y < 2; ++y) {
+                const int r = i + x, col = c + y;
+                const cplx<float> u = Us[r * Np + col];
+                // subtract lambda u exactly, then round the residual once
+                DF qr = sr[x][y], qi = si[x][y];
+                df_add_prod(qr, -ls[col], u.re);
+                df_add_prod(qi, -ls[col], u.im);
+                Rs[r * Np + col] = mk(qr.s + (qr.c + lo[x][y].re), qi.s + (qi.c + lo[x][y].im));
+            }
     }
     __syncthreads();
     // P = U^dag R (FP32)
     smem_cgemm<float, true>(Np, Np, Us, Rs, Ps, tid, nt);
     for (int n = tid; n < N; n += nt) {
-        double s = 0.0;
+        double sq = 0.0;
         for (int l = 0; l < N; ++l) {
             const cplx<float> u = Us[l * Np + n];
-            s += (double)u.re * u.re + (double)u.im * u.im;
+            sq += (double)u.re * u.re + (double)u.im * u.im;
         }
-        Sn[n] = s;
+        Sn[n] = sq;
     }
     __syncthreads();
     for (int n = tid; n < N; n += nt) rho[n] = (double)ls[n] + (double)Ps[n * Np + n].re / Sn[n];
@@ -418,7 +425,7 @@ __global__ void __launch_bounds__(256) refine_kernel(int N, const cplx<double>* 
         if (bad || !isfinite(e2)) s_flag = 1;
     }
     __syncthreads();
-    // C in place of P (zero diagonal and zero for flagged gaps)
+    // C1 into Rs; X (P without its diagonal) stays in Ps
     for (int e = tid; e < NPP; e += nt) {
         const int m = e / Np, n = e % Np;
         cplx<float> c = mk(0.f, 0.f);
@@ -426,11 +433,33 @@ __global__ void __launch_bounds__(256) refine_kernel(int N, const cplx<double>* 
             const double d = rho[n] - rho[m];
             if (fabs(d) > degen_gap) c = mk((float)((double)Ps[e].re / d), (float)((double)Ps[e].im / d));
         }
-        Ps[e] = c;
+        Rs[e] = c;
+        if (m == n) Ps[e] = mk(0.f, 0.f);
     }
     __syncthreads();
-    // U' = U + U C (FP32) into Rs
-    smem_cgemm<float, false>(Np, Np, Us, Ps, Rs, tid, nt);
+    // X C1 into Hh (H is no longer needed); diagonal of the normalisation term
+    smem_cgemm<float, false>(Np, Np, Ps, Rs, Hh, tid, nt);
+    for (int n = tid; n < Np; n += nt) {
+        double q = 0.0;
+        for (int m = 0; m < N; ++m) q += (double)abs2(Rs[m * Np + n]);
+        Dn[n] = -0.5 * q;
+    }
+    __syncthreads();
+    // C = C1 + C2 into Rs
+    for (int e = tid; e < NPP; e += nt) {
+        const int m = e / Np, n = e % Np;
+        if (m >= N || n >= N) continue;
+        if (m == n) {
+            Rs[e] = mk((float)Dn[n], 0.f);
+        } else {
+            const double d = rho[n] - rho[m];
+            if (fabs(d) > degen_gap)
+                Rs[e] = Rs[e] + mk((float)((double)Hh[e].re / d), (float)((double)Hh[e].im / d));
+        }
+    }
+    __syncthreads();
+    // U C into Ps
+    smem_cgemm<float, false>(Np, Np, Us, Rs, Ps, tid, nt);
     __syncthreads();
     for (int n = tid; n < N; n += nt) {
         const double en = En[n];
@@ -439,7 +468,7 @@ __global__ void __launch_bounds__(256) refine_kernel(int N, const cplx<double>* 
         E64[(size_t)k * N + rank] = en;
         const float sc = (float)(1.0 / sqrt(Sn[n]));
         for (int row = 0; row < N; ++row) {
-            const cplx<float> u = Us[row * Np + n] + Rs[row * Np + n];
+            const cplx<float> u = Us[row * Np + n] + Ps[row * Np + n];
             U[(size_t)k * NN + row * N + rank] = mk(u.re * sc, u.im * sc);
         }
     }
@@ -449,7 +478,7 @@ __global__ void __launch_bounds__(256) refine_kernel(int N, const cplx<double>* 
 
 size_t refine_smem_bytes(int N) {
     const size_t Np = N + (N & 1);
-    return Np * Np * sizeof(cplx<double>) + 3 * Np * sizeof(double) + 3 * Np * Np * sizeof(cplx<float>);
+    return 4 * Np * sizeof(double) + 5 * Np * Np * sizeof(cplx<float>);
 }
 
 cudaError_t launch_refine(int N, int64_t nk, const cplx<double>* H64, const float* lam, cplx<float>* U, double* E64,

@@ -16,8 +16,9 @@
 //
 // Precision: the plan is built in FP64.  The FP64 form keeps G2 in FP64 for all
 // blocks.  The mixed form keeps all blocks in FP32 (nbz-term sums of FP32
-// values, about 1e-7 relative) plus block 0 (H) in FP64 for the FP64 eigenpair
-// refinement.
+// values, about 1e-7 relative) for its per-k work, plus FP64 slabs for the FP64
+// H(k) of the eigenpair refinement and for its FP64 reruns (all blocks when
+// they fit in memory, else H alone).
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -42,11 +43,12 @@ __device__ __forceinline__ cplx<double> phase(double k, int R) {
 __global__ void sep_stage_a(const cplx<double>* __restrict__ box, cplx<double>* __restrict__ G1, int EL, int nbx,
                             int nby, int nbz, int rx0, int n1) {
     const int yz = blockIdx.y, qx = blockIdx.z;
-    const double kx = mp_coord(qx, n1);
+    __shared__ cplx<double> ph[32];
+    if (threadIdx.x < nbx) ph[threadIdx.x] = phase(mp_coord(qx, n1), rx0 + (int)threadIdx.x);
+    __syncthreads();
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < EL; e += gridDim.x * blockDim.x) {
         cplx<double> acc = mk(0.0, 0.0);
-        for (int ix = 0; ix < nbx; ++ix)
-            fma_c(acc, phase(kx, rx0 + ix), box[((size_t)ix * nby * nbz + yz) * EL + e]);
+        for (int ix = 0; ix < nbx; ++ix) fma_c(acc, ph[ix], box[((size_t)ix * nby * nbz + yz) * EL + e]);
         G1[((size_t)qx * nby * nbz + yz) * EL + e] = acc;
     }
 }
@@ -57,19 +59,30 @@ __global__ void sep_stage_b(const cplx<double>* __restrict__ G1, cplx<double>* _
                             cplx<float>* __restrict__ G2f, int NN, int nbk, int nbd, int nby, int nbz, int ry0, int n1,
                             int n2) {
     const int iz = blockIdx.y % nbz, qy = blockIdx.y / nbz, qx = blockIdx.z;
-    const double ky = mp_coord(qy, n2);
+    __shared__ cplx<double> ph[32];
+    if (threadIdx.x < nby) ph[threadIdx.x] = phase(mp_coord(qy, n2), ry0 + (int)threadIdx.x);
+    __syncthreads();
     const int EL = nbk * NN;
     const size_t cell = ((size_t)qx * n2 + qy) * nbz + iz;
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < EL; e += gridDim.x * blockDim.x) {
         cplx<double> acc = mk(0.0, 0.0);
-        for (int iy = 0; iy < nby; ++iy)
-            fma_c(acc, phase(ky, ry0 + iy), G1[(((size_t)qx * nby + iy) * nbz + iz) * EL + e]);
+        for (int iy = 0; iy < nby; ++iy) fma_c(acc, ph[iy], G1[(((size_t)qx * nby + iy) * nbz + iz) * EL + e]);
         if (e < nbd * NN) G2d[cell * nbd * NN + e] = acc;
         if (G2f) G2f[cell * EL + e] = mk((float)acc.re, (float)acc.im);
     }
 }
 
-constexpr int kSepItems = 2;  // k-points per CTA in the per-k stages
+// Upper-triangle element u (row-major over n <= m) -> (n, m).  Row n holds
+// N - n elements and starts at off(n) = n (2N - n + 1) / 2.
+__device__ __forceinline__ void upper_pair(int u, int N, int& n, int& mm) {
+    const float b = 2.f * N + 1.f;
+    int r = (int)((b - sqrtf(b * b - 8.f * u)) * 0.5f);
+    r = r < 0 ? 0 : (r > N - 1 ? N - 1 : r);
+    while (r > 0 && r * (2 * N - r + 1) / 2 > u) --r;
+    while (r < N - 1 && (r + 1) * (2 * N - r) / 2 <= u) ++r;
+    n = r;
+    mm = r + (u - r * (2 * N - r + 1) / 2);
+}
 
 __device__ __forceinline__ void item_coords(const KRange& kr, int64_t i, int q[3], double k[3]) {
     const int64_t ki = k_of(kr, i);
@@ -79,96 +92,189 @@ __device__ __forceinline__ void item_coords(const KRange& kr, int64_t i, int q[3
     for (int a = 0; a < 3; ++a) k[a] = mp_coord(q[a], kr.mp[a]);
 }
 
-// W[i][blk][pair] for all stack blocks: X_b = sum_iz phase(kz) G2[qx][qy][iz][b][pair]
-// accumulated in TG, then the tight-binding epilogue in FP64.
-template <typename T, typename TG, int NB>
-__global__ void __launch_bounds__(256) sep_w_kernel(DevModel m, KRange kr, const cplx<TG>* __restrict__ G2, int nbz,
-                                                    int rz0, cplx<T>* __restrict__ W) {
-    const int NN = m.N * m.N;
-    __shared__ cplx<TG> ph[kSepItems][32];
-    __shared__ double ks[kSepItems][3];
-    __shared__ int qs[kSepItems][2];
-    const int64_t i0 = (int64_t)blockIdx.x * kSepItems;
-    if (threadIdx.x < kSepItems) {
-        const int64_t i = i0 + threadIdx.x;
+// Per-CTA item header: k, kz phases and slab offset of KI consecutive items,
+// and whether they all lie in one (qx, qy) column (then each slab element is
+// loaded once and applied to all KI items).
+template <typename TG, int KI>
+struct ItemHead {
+    cplx<TG> ph[KI][32];
+    cplx<TG> phi[KI][kMaxN];   // exp(2 pi i k.tau_n); psi_nm = conj(phi_n) phi_m
+    double k[KI][3];
+    size_t slab[KI];
+    int n_items;
+    int uniform;
+};
+
+template <typename TG, int KI>
+__device__ void load_items(ItemHead<TG, KI>& h, const KRange& kr, int nbz, int rz0, size_t slab_elems,
+                           const double* __restrict__ tau, int N) {
+    const int64_t i0 = (int64_t)blockIdx.x * KI;
+    if (threadIdx.x == 0) h.n_items = (int)(kr.count - i0 < KI ? kr.count - i0 : KI);
+    if (threadIdx.x < KI) {
+        const int it = threadIdx.x;
         int q[3] = {0, 0, 0};
         double k[3] = {0.0, 0.0, 0.0};
-        if (i < kr.count) item_coords(kr, i, q, k);
-        ks[threadIdx.x][0] = k[0]; ks[threadIdx.x][1] = k[1]; ks[threadIdx.x][2] = k[2];
-        qs[threadIdx.x][0] = q[0]; qs[threadIdx.x][1] = q[1];
+        if (i0 + it < kr.count) item_coords(kr, i0 + it, q, k);
+        h.k[it][0] = k[0]; h.k[it][1] = k[1]; h.k[it][2] = k[2];
+        h.slab[it] = ((size_t)q[0] * kr.mp[1] + q[1]) * slab_elems;
     }
     __syncthreads();
-    for (int e = threadIdx.x; e < kSepItems * 32; e += blockDim.x) {
+    if (threadIdx.x == 0) {
+        int u = 1;
+        for (int it = 1; it < h.n_items; ++it) u &= (h.slab[it] == h.slab[0]) ? 1 : 0;
+        h.uniform = u;
+    }
+    for (int e = threadIdx.x; e < KI * 32; e += blockDim.x) {
         const int it = e / 32, iz = e % 32;
-        cplx<double> p = iz < nbz ? phase(ks[it][2], rz0 + iz) : mk(0.0, 0.0);
-        ph[it][iz] = mk((TG)p.re, (TG)p.im);
+        const cplx<double> p = iz < nbz ? phase(h.k[it][2], rz0 + iz) : mk(0.0, 0.0);
+        h.ph[it][iz] = mk((TG)p.re, (TG)p.im);
     }
+    if (tau)
+        for (int e = threadIdx.x; e < KI * N; e += blockDim.x) {
+            const int it = e / N, n = e % N;
+            double s, c;
+            sincospi(2.0 * (h.k[it][0] * tau[3 * n] + h.k[it][1] * tau[3 * n + 1] + h.k[it][2] * tau[3 * n + 2]), &s, &c);
+            h.phi[it][n] = mk((TG)c, (TG)s);
+        }
     __syncthreads();
-    for (int it = 0; it < kSepItems; ++it) {
-        const int64_t i = i0 + it;
-        if (i >= kr.count) break;
-        const cplx<TG>* g = G2 + ((size_t)qs[it][0] * kr.mp[1] + qs[it][1]) * nbz * NB * NN;
-        const double k[3] = {ks[it][0], ks[it][1], ks[it][2]};
-        for (int pair = threadIdx.x; pair < NN; pair += blockDim.x) {
-            cplx<TG> acc[NB];
+}
+
+// acc[it] = sum_iz ph[it][iz] g[slab(it) + iz * zstride]
+template <typename TG, int KI>
+__device__ __forceinline__ void column_sum(const ItemHead<TG, KI>& h, const cplx<TG>* __restrict__ g, size_t zstride,
+                                           int nbz, cplx<TG> (&acc)[KI]) {
 #pragma unroll
-            for (int b = 0; b < NB; ++b) acc[b] = mk((TG)0, (TG)0);
-            for (int iz = 0; iz < nbz; ++iz) {
-                const cplx<TG> p = ph[it][iz];
-                const cplx<TG>* gz = g + (size_t)iz * NB * NN + pair;
+    for (int it = 0; it < KI; ++it) acc[it] = mk((TG)0, (TG)0);
+    if (h.uniform) {
+        const cplx<TG>* gp = g + h.slab[0];
+        for (int iz = 0; iz < nbz; ++iz) {
+            const cplx<TG> v = gp[(size_t)iz * zstride];
 #pragma unroll
-                for (int b = 0; b < NB; ++b) fma_c(acc[b], p, gz[(size_t)b * NN]);
+            for (int it = 0; it < KI; ++it) fma_c(acc[it], h.ph[it][iz], v);
+        }
+    } else {
+#pragma unroll
+        for (int it = 0; it < KI; ++it)
+            if (it < h.n_items)
+                for (int iz = 0; iz < nbz; ++iz) fma_c(acc[it], h.ph[it][iz], g[h.slab[it] + (size_t)iz * zstride]);
+    }
+}
+
+// W[i][blk][pair] for KI items x a tile of blockDim pairs, with the
+// tight-binding epilogue in TG (psi_nm = conj(phi_n) phi_m from N phases per
+// k-point, dt = C (tau_m - tau_n)):
+//     H = psi X_0,  A_b = psi X_{4+b}                 (staged in shared memory)
+//     H_a = i (psi X_{1+a} + dt_a H),  Om_q = i (psi X_{7+q} + dt_qa A_qb - dt_qb A_qa)
+// Each thread reads back only its own staged values.  Only the upper triangle
+// (n <= m) of each block is formed: every block is Hermitian and its consumers
+// (the eigensolver, the rotation) read that triangle.  The FP32 H block is not
+// written in the mixed form: its Jacobi reads the FP64 H(k).
+template <typename T, typename TG, int NB, int KI>
+__global__ void __launch_bounds__(128) sep_w_kernel(DevModel m, KRange kr, const cplx<TG>* __restrict__ G2, int nbz,
+                                                    int rz0, cplx<T>* __restrict__ W) {
+    extern __shared__ unsigned char smem_raw[];
+    cplx<TG>* Xs = reinterpret_cast<cplx<TG>*>(smem_raw);  // [H, A_x, A_y, A_z][KI][blockDim]
+    __shared__ ItemHead<TG, KI> h;
+    const int NN = m.N * m.N, PT = blockDim.x, t = threadIdx.x;
+    load_items<TG, KI>(h, kr, nbz, rz0, (size_t)nbz * NB * NN, m.has_tau ? m.tau : nullptr, m.N);
+    // every block is Hermitian and its consumers read the upper triangle:
+    // threads walk the N (N + 1) / 2 elements n <= m
+    const int u = blockIdx.y * PT + t;
+    if (u >= m.N * (m.N + 1) / 2) return;
+    int n, mm;
+    upper_pair(u, m.N, n, mm);
+    const int pair = n * m.N + mm;
+    TG dt[3] = {(TG)0, (TG)0, (TG)0};
+    cplx<TG> psi[KI];
+#pragma unroll
+    for (int it = 0; it < KI; ++it) psi[it] = mk((TG)1, (TG)0);
+    if (m.has_tau) {
+        double d[3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) d[i] = m.tau[mm * 3 + i] - m.tau[n * 3 + i];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) dt[a] = (TG)(m.C[a * 3 + 0] * d[0] + m.C[a * 3 + 1] * d[1] + m.C[a * 3 + 2] * d[2]);
+#pragma unroll
+        for (int it = 0; it < KI; ++it) psi[it] = cj_mul(h.phi[it][n], h.phi[it][mm]);
+    }
+    const int64_t i0 = (int64_t)blockIdx.x * KI;
+    auto Wp = [&](int it, int b) { return W + ((size_t)(i0 + it) * NB + b) * NN + pair; };
+    auto Xp = [&](int slot, int it) -> cplx<TG>& { return Xs[((size_t)slot * KI + it) * PT + t]; };
+    cplx<TG> acc[KI];
+    // H, then the connection A_b
+    column_sum<TG, KI>(h, G2 + pair, (size_t)NB * NN, nbz, acc);
+#pragma unroll
+    for (int it = 0; it < KI; ++it) {
+        const cplx<TG> v = psi[it] * acc[it];
+        Xp(0, it) = v;
+        if (sizeof(T) == 8 && it < h.n_items) *Wp(it, 0) = mk((T)v.re, (T)v.im);
+    }
+    if constexpr (NB == 10) {
+#pragma unroll
+        for (int b = 0; b < 3; ++b) {
+            column_sum<TG, KI>(h, G2 + (size_t)(4 + b) * NN + pair, (size_t)NB * NN, nbz, acc);
+#pragma unroll
+            for (int it = 0; it < KI; ++it) {
+                const cplx<TG> v = psi[it] * acc[it];
+                Xp(1 + b, it) = v;
+                if (it < h.n_items) *Wp(it, 4 + b) = mk((T)v.re, (T)v.im);
             }
-            cplx<double> X[NB];
+        }
+    }
+    // H_a
 #pragma unroll
-            for (int b = 0; b < NB; ++b) X[b] = mk((double)acc[b].re, (double)acc[b].im);
-            ft_epilogue<T, NB>(m, k, pair, X, W + (size_t)i * NB * NN, NN);
+    for (int a = 0; a < 3; ++a) {
+        column_sum<TG, KI>(h, G2 + (size_t)(1 + a) * NN + pair, (size_t)NB * NN, nbz, acc);
+#pragma unroll
+        for (int it = 0; it < KI; ++it) {
+            const cplx<TG> v = times_i(psi[it] * acc[it] + dt[a] * Xp(0, it));
+            if (it < h.n_items) *Wp(it, 1 + a) = mk((T)v.re, (T)v.im);
+        }
+    }
+    // Omega_q, q = (x,y), (x,z), (y,z)
+    if constexpr (NB == 10) {
+        constexpr int qa[3] = {0, 0, 1}, qb[3] = {1, 2, 2};
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            column_sum<TG, KI>(h, G2 + (size_t)(7 + q) * NN + pair, (size_t)NB * NN, nbz, acc);
+#pragma unroll
+            for (int it = 0; it < KI; ++it) {
+                const cplx<TG> v = times_i(psi[it] * acc[it] + dt[qa[q]] * Xp(1 + qb[q], it) - dt[qb[q]] * Xp(1 + qa[q], it));
+                if (it < h.n_items) *Wp(it, 7 + q) = mk((T)v.re, (T)v.im);
+            }
         }
     }
 }
 
-// H64[i][pair] = psi * sum_iz phase(kz) G2d[qx][qy][iz][0][pair]
-__global__ void __launch_bounds__(256) sep_h64_kernel(const cplx<double>* __restrict__ G2, KRange kr, int N, int nbd,
+// H64[i][pair] = psi * sum_iz phase(kz) G2d[qx][qy][iz][0][pair] for KI items
+template <int KI>
+__global__ void __launch_bounds__(128) sep_h64_kernel(const cplx<double>* __restrict__ G2, KRange kr, int N, int nbd,
                                                       int nbz, int rz0, const double* __restrict__ tau,
                                                       cplx<double>* __restrict__ H64) {
+    __shared__ ItemHead<double, KI> h;
     const int NN = N * N;
-    __shared__ cplx<double> ph[kSepItems][32];
-    __shared__ double ks[kSepItems][3];
-    __shared__ int qs[kSepItems][2];
-    const int64_t i0 = (int64_t)blockIdx.x * kSepItems;
-    if (threadIdx.x < kSepItems) {
-        const int64_t i = i0 + threadIdx.x;
-        int q[3] = {0, 0, 0};
-        double k[3] = {0.0, 0.0, 0.0};
-        if (i < kr.count) item_coords(kr, i, q, k);
-        ks[threadIdx.x][0] = k[0]; ks[threadIdx.x][1] = k[1]; ks[threadIdx.x][2] = k[2];
-        qs[threadIdx.x][0] = q[0]; qs[threadIdx.x][1] = q[1];
-    }
-    __syncthreads();
-    for (int e = threadIdx.x; e < kSepItems * 32; e += blockDim.x) {
-        const int it = e / 32, iz = e % 32;
-        ph[it][iz] = iz < nbz ? phase(ks[it][2], rz0 + iz) : mk(0.0, 0.0);
-    }
-    __syncthreads();
-    for (int it = 0; it < kSepItems; ++it) {
-        const int64_t i = i0 + it;
-        if (i >= kr.count) break;
-        const cplx<double>* g = G2 + ((size_t)qs[it][0] * kr.mp[1] + qs[it][1]) * nbz * nbd * NN;
-        for (int pair = threadIdx.x; pair < NN; pair += blockDim.x) {
-            cplx<double> acc = mk(0.0, 0.0);
-            for (int iz = 0; iz < nbz; ++iz) fma_c(acc, ph[it][iz], g[(size_t)iz * nbd * NN + pair]);
-            if (tau) {
-                const int n = pair / N, mm = pair % N;
-                const double x = ks[it][0] * (tau[mm * 3] - tau[n * 3]) + ks[it][1] * (tau[mm * 3 + 1] - tau[n * 3 + 1]) +
-                                 ks[it][2] * (tau[mm * 3 + 2] - tau[n * 3 + 2]);
-                double s, c;
-                sincospi(2.0 * x, &s, &c);
-                acc = mk(c, s) * acc;
-            }
-            H64[(size_t)i * NN + pair] = acc;
-        }
+    load_items<double, KI>(h, kr, nbz, rz0, (size_t)nbz * nbd * NN, tau, N);
+    // H is Hermitian and the eigensolver and refinement read its upper triangle
+    const int u = blockIdx.y * blockDim.x + threadIdx.x;
+    if (u >= N * (N + 1) / 2) return;
+    int n, mm;
+    upper_pair(u, N, n, mm);
+    const int pair = n * N + mm;
+    cplx<double> acc[KI];
+    column_sum<double, KI>(h, G2 + pair, (size_t)nbd * NN, nbz, acc);
+    const int64_t i0 = (int64_t)blockIdx.x * KI;
+#pragma unroll
+    for (int it = 0; it < KI; ++it) {
+        if (it >= h.n_items) break;
+        cplx<double> v = acc[it];
+        if (tau) v = cj_mul(h.phi[it][n], h.phi[it][mm]) * v;
+        H64[(size_t)(i0 + it) * NN + pair] = v;
     }
 }
+
+constexpr int kItemsF = 8;   // items per CTA with FP32 slabs
+constexpr int kItemsD = 4;   // items per CTA with FP64 slabs
+constexpr int kItemsH = 8;   // items per CTA of the FP64 H sums
 
 }  // namespace
 
@@ -187,17 +293,26 @@ int sep_plan_build(SepPlan& p, const DevModel& m, const double* R_host, const cp
     const int nb[3] = {hi[0] - lo[0] + 1, hi[1] - lo[1] + 1, hi[2] - lo[2] + 1};
     if (nb[0] > 32 || nb[1] > 32 || nb[2] > 32) return 1;
     const int NN = m.N * m.N, nbk = m.nb, EL = nbk * NN;
-    const int nbd = fp64 ? nbk : 1;
     const size_t box = (size_t)nb[0] * nb[1] * nb[2];
     const size_t slabs = (size_t)mp[0] * mp[1] * nb[2];
-    const size_t g2d_bytes = slabs * nbd * NN * sizeof(cplx<double>);
     const size_t g2f_bytes = fp64 ? 0 : slabs * EL * sizeof(cplx<float>);
     const size_t g1_bytes = (size_t)mp[0] * nb[1] * nb[2] * EL * sizeof(cplx<double>);
     const size_t box_bytes = box * EL * sizeof(cplx<double>);
     size_t free_b = 0, total_b = 0;
     if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return 2;
-    // the slabs stay resident for the run; leave room for the per-chunk buffers
-    if (g2d_bytes + g2f_bytes + g1_bytes + box_bytes > free_b / 2) return 1;
+    // The slabs stay resident for the run; leave room for the per-chunk
+    // buffers.  The mixed form keeps FP64 slabs of every block when they fit
+    // (its FP64 reruns then take the separable sums too), else of H alone.
+    auto fits = [&](int nbd_) {
+        return slabs * nbd_ * NN * sizeof(cplx<double>) + g2f_bytes + g1_bytes + box_bytes <= free_b / 2;
+    };
+    int nbd = nbk;
+    if (!fits(nbd)) {
+        if (fp64) return 1;
+        nbd = 1;
+        if (!fits(nbd)) return 1;
+    }
+    const size_t g2d_bytes = slabs * nbd * NN * sizeof(cplx<double>);
     std::vector<cplx<double>> hb(box * EL, mk(0.0, 0.0));
     for (int r = 0; r < m.nR; ++r) {
         const int ix = (int)std::lrint(R_host[3 * r]) - lo[0], iy = (int)std::lrint(R_host[3 * r + 1]) - lo[1],
@@ -250,31 +365,41 @@ void sep_plan_free(SepPlan& p) {
     p = SepPlan();
 }
 
+namespace {
+inline int pair_tile(int n_elem) { return n_elem >= 128 ? 128 : ((n_elem + 31) / 32) * 32; }
+
+template <typename T, typename TG, int NB, int KI>
+cudaError_t launch_w(const DevModel& m, const KRange& kr, const cplx<TG>* G2, int nbz, int rz0, cplx<T>* W,
+                     cudaStream_t s) {
+    const int NU = m.N * (m.N + 1) / 2, PT = pair_tile(NU);
+    const size_t smem = (size_t)(NB == 10 ? 4 : 1) * KI * PT * sizeof(cplx<TG>);
+    cudaError_t e = cudaFuncSetAttribute(sep_w_kernel<T, TG, NB, KI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    dim3 grid((unsigned)((kr.count + KI - 1) / KI), (unsigned)((NU + PT - 1) / PT));
+    sep_w_kernel<T, TG, NB, KI><<<grid, PT, smem, s>>>(m, kr, G2, nbz, rz0, W);
+    return cudaGetLastError();
+}
+}  // namespace
+
 cudaError_t launch_sep_h64(const SepPlan& p, const KRange& kr, cplx<double>* H64, cudaStream_t s) {
     if (kr.count <= 0) return cudaSuccess;
-    const unsigned grid = (unsigned)((kr.count + kSepItems - 1) / kSepItems);
-    sep_h64_kernel<<<grid, 256, 0, s>>>(p.G2d, kr, p.N, p.nbd, p.nb[2], p.lo[2], p.tau, H64);
+    const int NU = p.N * (p.N + 1) / 2, PT = pair_tile(NU);
+    dim3 grid((unsigned)((kr.count + kItemsH - 1) / kItemsH), (unsigned)((NU + PT - 1) / PT));
+    sep_h64_kernel<kItemsH><<<grid, PT, 0, s>>>(p.G2d, kr, p.N, p.nbd, p.nb[2], p.lo[2], p.tau, H64);
     return cudaGetLastError();
 }
 
 template <typename T>
 cudaError_t launch_sep_w(const SepPlan& p, const DevModel& m, const KRange& kr, cplx<T>* W, cudaStream_t s) {
     if (kr.count <= 0) return cudaSuccess;
-    const unsigned grid = (unsigned)((kr.count + kSepItems - 1) / kSepItems);
-    const int threads = m.N <= 8 ? 64 : 256;
-    if (p.fp64) {
-        if (m.nb == 10)
-            sep_w_kernel<T, double, 10><<<grid, threads, 0, s>>>(m, kr, p.G2d, p.nb[2], p.lo[2], W);
-        else
-            sep_w_kernel<T, double, 4><<<grid, threads, 0, s>>>(m, kr, p.G2d, p.nb[2], p.lo[2], W);
-    } else {
-        if (sizeof(T) == 8) return cudaErrorInvalidValue;  // FP64 output needs the FP64 slabs
-        if (m.nb == 10)
-            sep_w_kernel<T, float, 10><<<grid, threads, 0, s>>>(m, kr, p.G2f, p.nb[2], p.lo[2], W);
-        else
-            sep_w_kernel<T, float, 4><<<grid, threads, 0, s>>>(m, kr, p.G2f, p.nb[2], p.lo[2], W);
+    if (sizeof(T) == 8) {
+        if (p.nbd != p.nbk) return cudaErrorInvalidValue;  // FP64 output needs FP64 slabs of every block
+        if (m.nb == 10) return launch_w<T, double, 10, kItemsD>(m, kr, p.G2d, p.nb[2], p.lo[2], W, s);
+        return launch_w<T, double, 4, kItemsD>(m, kr, p.G2d, p.nb[2], p.lo[2], W, s);
     }
-    return cudaGetLastError();
+    if (m.nb == 10) return launch_w<T, float, 10, kItemsF>(m, kr, p.G2f, p.nb[2], p.lo[2], W, s);
+    return launch_w<T, float, 4, kItemsF>(m, kr, p.G2f, p.nb[2], p.lo[2], W, s);
 }
 
 template cudaError_t launch_sep_w<double>(const SepPlan&, const DevModel&, const KRange&, cplx<double>*, cudaStream_t);

@@ -20,57 +20,88 @@ namespace mepi {
 
 namespace {
 
+// The six rotated blocks of one k-point (Hbar_x,y,z, Abar_x,y,z): staged in
+// shared memory as real and imaginary planes with row stride N + 1, so that
+// both row and column walks are free of bank conflicts, or, when they do not
+// fit (FP64 beyond N = 46), read from global memory.
 template <typename T>
-struct GaugeCtx {
-    const cplx<T>* HA;  // [6][N][N] of this k
-    const T* invd;      // [N][N] 1/(E_m - E_n) where D is defined, else 0 (shared memory)
-    int N, semantics;
+struct GaugeSm {
+    T* re;
+    T* im;
+    const cplx<T>* glob;
+    const T* invd;   // [N][N] 1/(E_m - E_n) where D is defined, else 0
+    int N, ld, semantics;
+    bool staged;
+    __device__ __forceinline__ cplx<T> X(int blk, int n, int m) const {
+        if (!staged) return glob[((size_t)blk * N + n) * N + m];
+        const int o = (blk * N + n) * ld + m;
+        return mk(re[o], im[o]);
+    }
     __device__ __forceinline__ cplx<T> D(int a, int n, int m) const {
         const T w = invd[n * N + m];
-        const cplx<T> h = HA[(size_t)a * N * N + n * N + m];
+        const cplx<T> h = X(a, n, m);
         return mk(h.re * w, h.im * w);
     }
     // A' used in the curvature commutators
     __device__ __forceinline__ cplx<T> Ac(int a, int n, int m) const {
-        cplx<T> ab = HA[(size_t)(3 + a) * N * N + n * N + m];
+        const cplx<T> ab = X(3 + a, n, m);
         if (semantics != 0) return ab;
         return ab + times_i(D(a, n, m));
     }
 };
 
 template <typename T>
+__device__ __forceinline__ T warp_sum_t(T v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+template <typename T>
 __global__ void __launch_bounds__(256) gauge_kernel(DevModel m, const double* __restrict__ Eg, const cplx<T>* __restrict__ HA,
                                                     const cplx<T>* __restrict__ OD, cplx<T>* __restrict__ V,
-                                                    T* __restrict__ CSV, cplx<T>* __restrict__ ODH) {
-    const int N = m.N, NN = N * N;
+                                                    T* __restrict__ CSV, cplx<T>* __restrict__ ODH, bool staged) {
+    const int N = m.N, NN = N * N, ld = N + 1;
     const int tid = threadIdx.x, nt = blockDim.x;
     const int64_t k = blockIdx.x;
     __shared__ double Es[kMaxN];
     __shared__ cplx<T> Oh[3][kMaxN];
     extern __shared__ unsigned char smem_raw[];
     T* invd = reinterpret_cast<T*>(smem_raw);
+    GaugeSm<T> g;
+    g.re = invd + NN;
+    g.im = g.re + 6 * N * ld;
+    g.invd = invd;
+    g.N = N;
+    g.ld = ld;
+    g.semantics = m.semantics;
+    g.staged = staged;
+    const int nblk = m.has_r ? 6 : 3;
+    const cplx<T>* HAk = HA + (size_t)k * 6 * NN;
+    g.glob = HAk;
     for (int n = tid; n < N; n += nt) Es[n] = Eg[(size_t)k * N + n];
+    for (int e = tid; e < (staged ? nblk * NN : 0); e += nt) {
+        const int blk = e / NN, r = e % NN;
+        const cplx<T> x = HAk[e];
+        const int o = (blk * N + r / N) * ld + r % N;
+        g.re[o] = x.re;
+        g.im[o] = x.im;
+    }
     __syncthreads();
-    // inverse gaps of the covariant derivative, decided and formed in FP64
+    // inverse gaps of the covariant derivative: the kuboTol decision in FP64
     for (int e = tid; e < NN; e += nt) {
         const int n = e / N, mm = e % N;
         const double ded = Es[mm] - Es[n];
-        invd[e] = (m.do_gauge && n != mm && fabs(ded) > m.kubo_tol) ? (T)(1.0 / ded) : (T)0;
+        invd[e] = (m.do_gauge && n != mm && fabs(ded) > m.kubo_tol) ? (T)1 / (T)ded : (T)0;
     }
     __syncthreads();
-    GaugeCtx<T> g;
-    g.HA = HA + (size_t)k * 6 * NN;
-    g.invd = invd;
-    g.N = N;
-    g.semantics = m.semantics;
     cplx<T>* Vk = V + (size_t)k * 3 * NN;
     // velocity
     for (int e = tid; e < 3 * NN; e += nt) {
-        int a = e / NN, p = (e / N) % N, q = e % N;
-        cplx<T> hb = g.HA[e];
+        const int a = e / NN, p = (e / N) % N, q = e % N;
+        const cplx<T> hb = g.X(a, p, q);
         cplx<T> v = hb;
         if (m.has_r && p != q) {
-            cplx<T> ab = g.HA[(size_t)(3 + a) * NN + p * N + q];
+            const cplx<T> ab = g.X(3 + a, p, q);
             cplx<T> av = ab;
             if (m.semantics == 0 || !m.do_gauge) av = ab + times_i(g.D(a, p, q));
             const T de = (T)(Es[q] - Es[p]);
@@ -82,18 +113,18 @@ __global__ void __launch_bounds__(256) gauge_kernel(DevModel m, const double* __
         for (int n = tid; n < N; n += nt) CSV[(size_t)k * N + n] = (T)0;
         return;
     }
-    // curvature diagonal
-    const int qa[3] = {0, 0, 1}, qb[3] = {1, 2, 2};
-    for (int t = tid; t < 3 * N; t += nt) {
-        int q = t / N, n = t % N;
-        int a = qa[q], b = qb[q];
+    // curvature diagonal: one warp per (q, n), lanes over the summed band m
+    const int lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+    for (int t = warp; t < 3 * N; t += nw) {
+        const int q = t / N, n = t % N;
+        const int a = q < 2 ? 0 : 1, b = q == 0 ? 1 : 2;   // (x,y), (x,z), (y,z)
         cplx<T> o = OD[((size_t)k * 3 + q) * N + n];
         if (m.do_gauge) {
             cplx<T> c1 = mk((T)0, (T)0), c2 = c1, c3 = c1;
-            for (int mm = 0; mm < N; ++mm) {
+            for (int mm = lane; mm < N; mm += 32) {
                 if (mm == n) continue;  // D has no diagonal, so the m = n terms vanish
-                cplx<T> Da_nm = g.D(a, n, mm), Da_mn = g.D(a, mm, n);
-                cplx<T> Db_nm = g.D(b, n, mm), Db_mn = g.D(b, mm, n);
+                const cplx<T> Da_nm = g.D(a, n, mm), Da_mn = g.D(a, mm, n);
+                const cplx<T> Db_nm = g.D(b, n, mm), Db_mn = g.D(b, mm, n);
                 // [D_a, A'_b]_nn
                 fma_c(c1, Da_nm, g.Ac(b, mm, n));
                 c1 = c1 - g.Ac(b, n, mm) * Da_mn;
@@ -104,16 +135,21 @@ __global__ void __launch_bounds__(256) gauge_kernel(DevModel m, const double* __
                 fma_c(c3, Da_nm, Db_mn);
                 c3 = c3 - Db_nm * Da_mn;
             }
+            c1 = mk(warp_sum_t(c1.re), warp_sum_t(c1.im));
+            c2 = mk(warp_sum_t(c2.re), warp_sum_t(c2.im));
+            c3 = mk(warp_sum_t(c3.re), warp_sum_t(c3.im));
             o = o - c1 + c2 - times_i(c3);
         }
-        Oh[q][n] = o;
-        if (ODH) ODH[((size_t)k * 3 + q) * N + n] = o;
+        if (lane == 0) {
+            Oh[q][n] = o;
+            if (ODH) ODH[((size_t)k * 3 + q) * N + n] = o;
+        }
     }
     __syncthreads();
     for (int n = tid; n < N; n += nt) {
-        cplx<T> om[3] = {(T)2 * Oh[2][n], (T)-2 * Oh[1][n], (T)2 * Oh[0][n]};
+        const cplx<T> om[3] = {(T)2 * Oh[2][n], (T)-2 * Oh[1][n], (T)2 * Oh[0][n]};
         cplx<T> acc = mk((T)0, (T)0);
-        for (int c = 0; c < 3; ++c) fma_cjc(acc, g.HA[(size_t)(3 + c) * NN + n * N + n], om[c]);
+        for (int c = 0; c < 3; ++c) fma_cjc(acc, g.X(3 + c, n, n), om[c]);
         CSV[(size_t)k * N + n] = (T)0.5 * acc.re;
     }
 }
@@ -125,10 +161,12 @@ cudaError_t launch_gauge(const DevModel& m, int64_t nk, const double* E, const c
                          cplx<T>* V, T* CSV, cplx<T>* ODH, cudaStream_t s) {
     if (nk <= 0) return cudaSuccess;
     int threads = m.N <= 16 ? 128 : 256;
-    const size_t smem = (size_t)m.N * m.N * sizeof(T);
+    size_t smem = ((size_t)m.N * m.N + 2 * 6 * (size_t)m.N * (m.N + 1)) * sizeof(T);
+    const bool staged = smem <= (size_t)220 * 1024;   // the opt-in limit is 227 KB, static arrays included
+    if (!staged) smem = (size_t)m.N * m.N * sizeof(T);
     cudaError_t e = cudaFuncSetAttribute(gauge_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    gauge_kernel<T><<<(unsigned)nk, threads, smem, s>>>(m, E, HA, OD, V, CSV, ODH);
+    gauge_kernel<T><<<(unsigned)nk, threads, smem, s>>>(m, E, HA, OD, V, CSV, ODH, staged);
     return cudaGetLastError();
 }
 

@@ -94,6 +94,93 @@ __device__ __forceinline__ void smem_cgemm(int N, int ld, const cplx<T>* __restr
     }
 }
 
+// Compensated FP32 arithmetic (Knuth's TwoSum, TwoProduct by FMA, and the
+// Dot2 summation of Ogita, Rump and Oishi, SIAM J. Sci. Comput. 26 (2005)):
+// a dot product of FP32 numbers accumulated as an unevaluated sum s + c, as if
+// in twice the working precision.  The _rn intrinsics are never contracted
+// into FMAs, which the error-free transformations rely on.
+struct DF {
+    float s, c;
+};
+__device__ __forceinline__ void df_add_prod(DF& acc, float a, float b) {
+    const float p = __fmul_rn(a, b);
+    const float pe = __fmaf_rn(a, b, -p);          // a b = p + pe exactly
+    const float t = __fadd_rn(acc.s, p);
+    const float bp = __fsub_rn(t, acc.s);
+    const float e = __fadd_rn(__fsub_rn(acc.s, __fsub_rn(t, bp)), __fsub_rn(p, bp));  // acc.s + p = t + e
+    acc.s = t;
+    acc.c = __fadd_rn(acc.c, __fadd_rn(e, pe));
+}
+
+// C = op(A) B for complex FP32 Np x Np matrices in shared memory (row stride
+// ld, Np even), accumulated in Dot2 so that the result is as if formed in
+// twice the working precision; 2 x 2 output tiles per thread.  op(A) = A^dag
+// when adjA.  Blo (optional) is a low-order part of B, added in plain FP32.
+// Chi receives the rounded result; Clo (optional) the remainder
+// (C = Chi + Clo to about 2^-44 relative).  With upper, only tiles with
+// i0 <= j0 are formed and the Hermitian mirror of the strictly upper ones is
+// written (for products known to be Hermitian).
+template <bool adjA>
+__device__ __forceinline__ void cgemm_dot2(int Np, int ld, const cplx<float>* __restrict__ A,
+                                           const cplx<float>* __restrict__ B, const cplx<float>* __restrict__ Blo,
+                                           cplx<float>* __restrict__ Chi, cplx<float>* __restrict__ Clo, bool upper,
+                                           int tid, int nt) {
+    const int h = Np >> 1;
+    for (int t = tid; t < h * h; t += nt) {
+        const int i0 = 2 * (t / h), j0 = 2 * (t % h);
+        if (upper && i0 > j0) continue;
+        DF re[2][2], im[2][2];
+        cplx<float> lo[2][2];
+#pragma unroll
+        for (int x = 0; x < 2; ++x)
+#pragma unroll
+            for (int y = 0; y < 2; ++y) {
+                re[x][y] = DF{0.f, 0.f};
+                im[x][y] = DF{0.f, 0.f};
+                lo[x][y] = mk(0.f, 0.f);
+            }
+        for (int l = 0; l < Np; ++l) {
+            cplx<float> a[2];
+            if (adjA) {
+                a[0] = conjg(A[l * ld + i0]);
+                a[1] = conjg(A[l * ld + i0 + 1]);
+            } else {
+                a[0] = A[i0 * ld + l];
+                a[1] = A[(i0 + 1) * ld + l];
+            }
+            const cplx<float> b[2] = {B[l * ld + j0], B[l * ld + j0 + 1]};
+#pragma unroll
+            for (int x = 0; x < 2; ++x)
+#pragma unroll
+                for (int y = 0; y < 2; ++y) {
+                    df_add_prod(re[x][y], a[x].re, b[y].re);
+                    df_add_prod(re[x][y], -a[x].im, b[y].im);
+                    df_add_prod(im[x][y], a[x].re, b[y].im);
+                    df_add_prod(im[x][y], a[x].im, b[y].re);
+                }
+            if (Blo) {
+                const cplx<float> bl[2] = {Blo[l * ld + j0], Blo[l * ld + j0 + 1]};
+#pragma unroll
+                for (int x = 0; x < 2; ++x)
+#pragma unroll
+                    for (int y = 0; y < 2; ++y) fma_c(lo[x][y], a[x], bl[y]);
+            }
+        }
+#pragma unroll
+        for (int x = 0; x < 2; ++x)
+#pragma unroll
+            for (int y = 0; y < 2; ++y) {
+                const int r = i0 + x, c = j0 + y;
+                const float cr = __fadd_rn(re[x][y].c, lo[x][y].re), ci = __fadd_rn(im[x][y].c, lo[x][y].im);
+                const float hr = __fadd_rn(re[x][y].s, cr), hi = __fadd_rn(im[x][y].s, ci);
+                if (upper && r > c) continue;   // the lower element of a diagonal tile comes from the mirror
+                Chi[r * ld + c] = mk(hr, hi);
+                if (Clo) Clo[r * ld + c] = mk(__fadd_rn(__fsub_rn(re[x][y].s, hr), cr), __fadd_rn(__fsub_rn(im[x][y].s, hi), ci));
+                if (upper && r < c) Chi[c * ld + r] = mk(hr, -hi);
+            }
+    }
+}
+
 // Which k-points a launch covers: k = list ? list[i] : k_begin + i * k_stride.
 struct KRange {
     int64_t k_begin, k_stride, count;
@@ -128,37 +215,32 @@ struct DevModel {
 };
 
 // Tight-binding phase epilogue of the Fourier sums for one (n,m) pair of one
-// k-point: from the raw sums X_b = sum_R exp(2 pi i k.R) S_b(R) it writes the
-// W-gauge blocks, with psi = exp(2 pi i k.(tau_m - tau_n)) and
+// k-point, in arithmetic TE: from the raw sums X_b = sum_R exp(2 pi i k.R) S_b(R)
+// it writes the W-gauge blocks, with psi = exp(2 pi i k.(tau_m - tau_n)) and
 // dt = C (tau_m - tau_n):
 //     H = psi X_0,  H_a = i (psi X_a + dt_a H),  A_b = psi X_{3+b},
 //     Om_ab = i (psi X_Q + dt_a A_b - dt_b A_a)
 // (the per-element angle 2 pi k.(R + tau_m - tau_n) of
 // src/wann_interp.f90:192-281 factorised; the Wannier convention is tau = 0).
-template <typename T, int NB>
-__device__ __forceinline__ void ft_epilogue(const DevModel& m, const double k[3], int pair, const cplx<double> (&X)[NB],
+template <typename T, typename TE, int NB>
+__device__ __forceinline__ void tb_epilogue(const DevModel& m, cplx<TE> psi, int pair, const cplx<TE> (&X)[NB],
                                             cplx<T>* __restrict__ Wk, int NN) {
-    const int n = pair / m.N, mm = pair % m.N;
-    cplx<double> psi = mk(1.0, 0.0);
-    double dt[3] = {0.0, 0.0, 0.0};
+    TE dt[3] = {(TE)0, (TE)0, (TE)0};
     if (m.has_tau) {
+        const int n = pair / m.N, mm = pair % m.N;
         double d[3];
         for (int i = 0; i < 3; ++i) d[i] = m.tau[mm * 3 + i] - m.tau[n * 3 + i];
-        double x = k[0] * d[0] + k[1] * d[1] + k[2] * d[2];
-        double s, c;
-        sincospi(2.0 * x, &s, &c);
-        psi = mk(c, s);
-        for (int a = 0; a < 3; ++a) dt[a] = m.C[a * 3 + 0] * d[0] + m.C[a * 3 + 1] * d[1] + m.C[a * 3 + 2] * d[2];
+        for (int a = 0; a < 3; ++a) dt[a] = (TE)(m.C[a * 3 + 0] * d[0] + m.C[a * 3 + 1] * d[1] + m.C[a * 3 + 2] * d[2]);
     }
-    cplx<double> H = psi * X[0];
+    const cplx<TE> H = psi * X[0];
     Wk[pair] = mk((T)H.re, (T)H.im);
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-        cplx<double> v = times_i(psi * X[1 + a] + dt[a] * H);
+        const cplx<TE> v = times_i(psi * X[1 + a] + dt[a] * H);
         Wk[(size_t)(1 + a) * NN + pair] = mk((T)v.re, (T)v.im);
     }
     if constexpr (NB == 10) {
-        cplx<double> A[3];
+        cplx<TE> A[3];
 #pragma unroll
         for (int b = 0; b < 3; ++b) {
             A[b] = psi * X[4 + b];
@@ -167,10 +249,26 @@ __device__ __forceinline__ void ft_epilogue(const DevModel& m, const double k[3]
         const int qa[3] = {0, 0, 1}, qb[3] = {1, 2, 2};
 #pragma unroll
         for (int q = 0; q < 3; ++q) {
-            cplx<double> v = times_i(psi * X[7 + q] + dt[qa[q]] * A[qb[q]] - dt[qb[q]] * A[qa[q]]);
+            const cplx<TE> v = times_i(psi * X[7 + q] + dt[qa[q]] * A[qb[q]] - dt[qb[q]] * A[qa[q]]);
             Wk[(size_t)(7 + q) * NN + pair] = mk((T)v.re, (T)v.im);
         }
     }
+}
+
+// The same with psi from the k-point itself (one sincospi per element).
+template <typename T, int NB>
+__device__ __forceinline__ void ft_epilogue(const DevModel& m, const double k[3], int pair, const cplx<double> (&X)[NB],
+                                            cplx<T>* __restrict__ Wk, int NN) {
+    cplx<double> psi = mk(1.0, 0.0);
+    if (m.has_tau) {
+        const int n = pair / m.N, mm = pair % m.N;
+        double x = 0.0;
+        for (int i = 0; i < 3; ++i) x += k[i] * (m.tau[mm * 3 + i] - m.tau[n * 3 + i]);
+        double s, c;
+        sincospi(2.0 * x, &s, &c);
+        psi = mk(c, s);
+    }
+    tb_epilogue<T, double, NB>(m, psi, pair, X, Wk, NN);
 }
 
 
@@ -219,8 +317,8 @@ cudaError_t launch_reduce(const double* partials, int n_cta, int size, double* o
 // G2[qx][qy][iz][blk][pair] stay resident in HBM for the run.
 struct SepPlan {
     bool ready = false;
-    bool fp64 = false;              // G2d holds all blocks (FP64 form); else G2f all + G2d block 0
-    int N = 0, nbk = 0, nbd = 0;    // n_wf, stack blocks, blocks in G2d
+    bool fp64 = false;              // built for the FP64 form (no FP32 slabs)
+    int N = 0, nbk = 0, nbd = 0;    // n_wf, stack blocks, blocks in G2d (nbk, or 1 = H alone)
     int mp[3] = {0, 0, 0}, lo[3] = {0, 0, 0}, nb[3] = {0, 0, 0};  // mesh, R box origin and size
     cplx<double>* G2d = nullptr;
     cplx<float>* G2f = nullptr;

@@ -8,7 +8,8 @@
 // curv_gaugeTrafo collapse to 3 diagonal-only rotations here plus O(N^2)
 // commutator diagonals in the gauge kernel.
 //
-// One k-point per CTA: U and the operand are staged in shared memory (padded
+// One k-point per CTA: U and the operand (mirrored from its upper triangle,
+// every W-gauge block being Hermitian) are staged in shared memory (padded
 // to an even size with zeros) and each product is an N x N x N complex
 // contraction in which every thread computes 2 x 2 output tiles
 // (smem_cgemm), so each shared-memory load feeds two multiply-adds.
@@ -19,16 +20,32 @@ namespace mepi {
 
 namespace {
 
+// A Hermitian W-gauge block into shared memory from its upper triangle (the
+// lower one is not formed by the separable Fourier sums).
+template <typename T>
+__device__ __forceinline__ void load_hermitian(const cplx<T>* __restrict__ Wb, cplx<T>* Xs, int N, int ld, int tid,
+                                               int nt) {
+    for (int e = tid; e < N * N; e += nt) {
+        const int i = e / N, c = e % N;
+        if (i > c) continue;
+        const cplx<T> x = Wb[e];
+        Xs[i * ld + c] = x;
+        if (i != c) Xs[c * ld + i] = conjg(x);
+    }
+}
+
 template <typename T>
 __global__ void __launch_bounds__(256) rot_kernel(DevModel m, const cplx<T>* __restrict__ W,
                                                   const cplx<T>* __restrict__ Ug, cplx<T>* __restrict__ HA,
                                                   cplx<T>* __restrict__ OD) {
     extern __shared__ unsigned char smem_raw[];
+    constexpr bool f32 = sizeof(T) == 4;
     const int N = m.N, NN = N * N;
-    const int Np = N + (N & 1), ld = Np;     // even padded size, zero padding
+    const int Np = N + (N & 1), ld = Np + 1;   // even padded size (zero padding), odd row stride
     cplx<T>* Us = reinterpret_cast<cplx<T>*>(smem_raw);
-    cplx<T>* Xs = Us + Np * Np;
-    cplx<T>* Ts = Xs + Np * Np;
+    cplx<T>* Xs = Us + Np * ld;
+    cplx<T>* Ts = Xs + Np * ld;
+    cplx<T>* Tl = Ts + Np * ld;   // FP32 form: low-order part of H_a U
     const int tid = threadIdx.x, nt = blockDim.x;
     const int64_t k = blockIdx.x;
     const int nbW = m.nb;
@@ -38,27 +55,46 @@ __global__ void __launch_bounds__(256) rot_kernel(DevModel m, const cplx<T>* __r
 
     if (!m.do_gauge) {
         for (int j = 0; j < nmat; ++j)
-            for (int e = tid; e < NN; e += nt) HAk[(size_t)j * NN + e] = Wk[(size_t)(1 + j) * NN + e];
+            for (int e = tid; e < NN; e += nt) {
+                const int i = e / N, c = e % N;
+                if (i > c) continue;
+                const cplx<T> x = Wk[(size_t)(1 + j) * NN + e];
+                HAk[(size_t)j * NN + e] = x;
+                if (i != c) HAk[(size_t)j * NN + c * N + i] = conjg(x);
+            }
         if (m.has_r)
             for (int q = 0; q < 3; ++q)
                 for (int n = tid; n < N; n += nt) OD[((size_t)k * 3 + q) * N + n] = Wk[(size_t)(7 + q) * NN + n * N + n];
         return;
     }
     const cplx<T> zero = mk((T)0, (T)0);
-    for (int e = tid; e < Np * Np; e += nt) {
-        const int i = e / Np, j = e % Np;
+    for (int e = tid; e < Np * ld; e += nt) {
+        const int i = e / ld, j = e % ld;
         Us[e] = (i < N && j < N) ? Ug[(size_t)k * NN + i * N + j] : zero;
         Xs[e] = zero;
         Ts[e] = zero;
+        if (f32) Tl[e] = zero;
     }
     // blocks 1..3 (H_a) and 4..6 (A_a): full rotation
     for (int j = 0; j < nmat; ++j) {
         __syncthreads();
-        for (int e = tid; e < NN; e += nt) Xs[(e / N) * ld + e % N] = Wk[(size_t)(1 + j) * NN + e];
+        load_hermitian(Wk + (size_t)(1 + j) * NN, Xs, N, ld, tid, nt);
         __syncthreads();
-        smem_cgemm<T, false>(N, ld, Xs, Us, Ts, tid, nt);          // T = X U
+        if constexpr (f32) {
+            if (j < 3) {
+                // the velocity blocks in Dot2: T = X U (hi + lo), then the
+                // Hermitian Y = U^dag T (upper triangle, mirrored)
+                cgemm_dot2<false>(Np, ld, Xs, Us, nullptr, Ts, Tl, false, tid, nt);
+                __syncthreads();
+                cgemm_dot2<true>(Np, ld, Us, Ts, Tl, Xs, nullptr, true, tid, nt);
+                __syncthreads();
+                for (int e = tid; e < NN; e += nt) HAk[(size_t)j * NN + e] = Xs[(e / N) * ld + e % N];
+                continue;
+            }
+        }
+        smem_cgemm<T, false>(Np, ld, Xs, Us, Ts, tid, nt);          // T = X U
         __syncthreads();
-        smem_cgemm<T, true>(N, ld, Us, Ts, Xs, tid, nt);           // Y = U^dag T (into Xs)
+        smem_cgemm<T, true>(Np, ld, Us, Ts, Xs, tid, nt);           // Y = U^dag T (into Xs)
         __syncthreads();
         for (int e = tid; e < NN; e += nt) HAk[(size_t)j * NN + e] = Xs[(e / N) * ld + e % N];
     }
@@ -66,9 +102,9 @@ __global__ void __launch_bounds__(256) rot_kernel(DevModel m, const cplx<T>* __r
     // blocks 7..9 (Omega_q): diagonal of U^dag Omega_q U only
     for (int q = 0; q < 3; ++q) {
         __syncthreads();
-        for (int e = tid; e < NN; e += nt) Xs[(e / N) * ld + e % N] = Wk[(size_t)(7 + q) * NN + e];
+        load_hermitian(Wk + (size_t)(7 + q) * NN, Xs, N, ld, tid, nt);
         __syncthreads();
-        smem_cgemm<T, false>(N, ld, Xs, Us, Ts, tid, nt);          // T = Omega U
+        smem_cgemm<T, false>(Np, ld, Xs, Us, Ts, tid, nt);          // T = Omega U
         __syncthreads();
         for (int n = tid; n < N; n += nt) {
             cplx<T> acc = zero;
@@ -85,7 +121,7 @@ cudaError_t launch_rot(const DevModel& m, int64_t nk, const cplx<T>* W, const cp
                        cudaStream_t s) {
     if (nk <= 0) return cudaSuccess;
     const int Np = m.N + (m.N & 1);
-    size_t smem = 3 * (size_t)Np * Np * sizeof(cplx<T>);
+    size_t smem = (sizeof(T) == 4 ? 4 : 3) * (size_t)Np * (Np + 1) * sizeof(cplx<T>);
     cudaError_t e = cudaFuncSetAttribute(rot_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     int threads = m.N <= 16 ? 128 : 256;

@@ -4,9 +4,12 @@ Tolerances (the plain form is all-FP64 and must match the reference's
 LAPACK-zheevd FP64 path):
   eigenvalues                 1e-10 relative to max |E|
   sigma_ab, MEP tensors       1e-8 relative to the largest entry of each tensor
-The mixed form (split-FP16 Fourier sums, FP32 per-k work, FP64 k-sums and FP64
-rerun of near-degenerate k-points) is held to 1e-6 relative on the k-summed
-tensors.
+The mixed form (separable Fourier sums from FP32 slabs with an FP64 H(k), FP32
+Jacobi plus the FP64 residual refinement, FP32 per-k work with FP64 energies,
+FP64 k-sums and an FP64 rerun of near-degenerate k-points) is held to 1e-6
+relative on the k-summed tensors.  Its tensor-core Fourier path (used for k
+lists off the mesh, forced here with MEPI_FT=tc) accumulates in FP32 inside the
+tensor core and is held to TC_TOL.
 """
 import os
 
@@ -22,6 +25,7 @@ pytestmark = pytest.mark.gpu
 KEYS = ["Ne_sum", "ahc", "mep_ic", "mep_lc", "mep_cs", "kubo_mep_ic", "kubo_mep_lc", "kubo_mep_cs"]
 GOLD = os.path.join(os.path.dirname(__file__), "golden", "femn.npz")
 E_TOL, SUM_TOL, MIXED_TOL = 1e-10, 1e-8, 1e-6
+TC_TOL = 2e-5   # FP32 accumulation over K = 2 nR inside the tensor core
 
 
 def rel(a, b):
@@ -181,6 +185,60 @@ def test_mixed_full_mesh_partition(gpu_lib):
         a = ctx.core_worker_loc(job, precision=api.PREC_MIXED, k_stride=stride)
         b = ctx.core_worker_loc(job, precision=api.PREC_FP64, k_stride=stride)
         check_sums(a, b, MIXED_TOL)
+
+
+def _wide_r_model():
+    """A model whose R box is wider than the separable sums take (|Rx| = 20)."""
+    m = random_tb_model(n_wf=8, r_max=1, seed=3)
+    n = m.n_wf
+    rng = np.random.default_rng(3)
+    t = 1e-3 * (rng.normal(size=(n, n)) + 1j * rng.normal(size=(n, n)))
+    rr = 1e-3 * (rng.normal(size=(3, n, n)) + 1j * rng.normal(size=(3, n, n)))
+    m.R_frac = np.vstack([m.R_frac, [[20.0, 0.0, 0.0], [-20.0, 0.0, 0.0]]])
+    m.H = np.concatenate([m.H, t[None], t.conj().T[None]])
+    m.r = np.concatenate([m.r, rr[None], np.conj(np.transpose(rr, (0, 2, 1)))[None]])
+    return m
+
+
+@pytest.mark.parametrize("case", ["tb", "wannier", "no_r", "wide_R"])
+def test_fourier_paths_fp64(gpu_lib, monkeypatch, case):
+    """The separable sums (default on a mesh) and the direct SIMT sums give the
+    same FP64 results, and both match the oracle; a model whose R box is too
+    wide for the separable form falls back to the direct sums."""
+    if case == "wide_R":
+        m = _wide_r_model()
+    else:
+        m = random_tb_model(n_wf=8, r_max=1, seed=7, with_r=(case != "no_r"), tb_convention=(case == "tb"))
+    job = dict(mp_grid=(6, 5, 4), ef_lst=np.array([-0.02, 0.0]), T_kelvin=0.0, valence_bands=4)
+    ref = O.run(m.as_dict(), job)
+    sep = api.run(m, job, precision=api.PREC_FP64)
+    monkeypatch.setenv("MEPI_FT", "simt")
+    simt = api.run(m, job, precision=api.PREC_FP64)
+    check_sums(sep, ref, SUM_TOL)
+    check_sums(simt, ref, SUM_TOL)
+    check_sums(sep, simt, 1e-10)
+
+
+def test_mixed_tensor_core_fourier(gpu_lib, monkeypatch):
+    model, job = workload("tb8_r1_k16")
+    ref = O.run(model.as_dict(), job, batch=512)
+    monkeypatch.setenv("MEPI_FT", "tc")
+    got = api.run(model, job, precision=api.PREC_MIXED)
+    check_sums(got, ref, TC_TOL)
+
+
+def test_mixed_partial_ownership(gpu_lib):
+    """A rank's share (k_begin, k_stride, k_count) walked in column order by the
+    separable sums covers exactly the oracle's k-points."""
+    m = random_tb_model(n_wf=10, r_max=2, decay=1.2, seed=9)
+    job = dict(mp_grid=(7, 6, 5), ef_lst=np.array([0.0]), T_kelvin=0.0, valence_bands=5)
+    kidx = 2 + 3 * np.arange(61)
+    ref = O.run(m.as_dict(), job, k_indices=kidx)
+    got = api.run(m, job, precision=api.PREC_MIXED, k_begin=2, k_stride=3, k_count=61)
+    assert got["n_k"] == 61
+    check_sums(got, ref, MIXED_TOL)
+    got64 = api.run(m, job, precision=api.PREC_FP64, k_begin=2, k_stride=3, k_count=61)
+    check_sums(got64, ref, SUM_TOL)
 
 
 def test_run_argument_errors(gpu_lib, model8):
