@@ -51,10 +51,15 @@ def parse():
     p.add_argument("--e2e-steps", type=int, default=2)
     p.add_argument("--cpu-sample", type=int, default=0, help="k-points for the CPU baseline (0 = about 15 s)")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--mesh", type=int, default=0,
+                   help="override the workload's mesh with an n^3 mesh (small cases for profiling; 0 = the workload's)")
+    p.add_argument("--chunk", type=int, default=0, help="k-points per chunk (0 = the library's default)")
     p.add_argument("--k-stride", type=int, default=1,
                    help="process every k-stride-th k-point of the mesh (small cases for profiling)")
-    p.add_argument("--fp64-check", type=int, default=65536,
-                   help="k-points of a strided subset on which the FP64 path is run for the error report (0 = off)")
+    p.add_argument("--fp64-check", type=int, default=-1,
+                   help="k-points on which the plain FP64 path is run for the error report and its own "
+                        "throughput: -1 = the whole mesh (reusing the timed mixed result), N > 0 = a strided "
+                        "subset of about N k-points, 0 = off")
     return p.parse_args()
 
 
@@ -230,6 +235,8 @@ def run_gpu(args, rank, world):
     from mepinterp_gb300.generator import workload
 
     model, job = workload(args.workload)
+    if args.mesh > 0:
+        job["mp_grid"] = (args.mesh,) * 3
     mp = job["mp_grid"]
     ks = max(1, args.k_stride)
     nk = (mp[0] * mp[1] * mp[2] + ks - 1) // ks
@@ -239,7 +246,7 @@ def run_gpu(args, rank, world):
     ctx = api.Context(model)
     plan_ms = None
     for w in range(max(args.warmup, 3)):
-        ctx.core_worker_loc(job, precision=prec, k_stride=ks)
+        ctx.core_worker_loc(job, precision=prec, k_stride=ks, chunk_k=args.chunk)
         if w == 0:
             plan_ms = ctx.timing()["plan_ms"]   # slab build of the first run on this mesh
     # timed region: exactly K steps, L2 flushed before each one
@@ -255,7 +262,7 @@ def run_gpu(args, rank, world):
     for _ in range(args.steps):
         flush.zero_()
         torch.cuda.synchronize()
-        res = ctx.core_worker_loc(job, precision=prec, k_stride=ks)
+        res = ctx.core_worker_loc(job, precision=prec, k_stride=ks, chunk_k=args.chunk)
         t = ctx.timing()
         run_ms.append(t["run_ms"])
         for key in api.STAGES:
@@ -277,7 +284,7 @@ def run_gpu(args, rank, world):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         with api.Context(model) as c2:
-            c2.core_worker_loc(job, precision=prec, k_stride=ks)
+            c2.core_worker_loc(job, precision=prec, k_stride=ks, chunk_k=args.chunk)
             t2 = c2.timing()
         e2e_times.append(time.perf_counter() - t0)
         h2d, d2h = t2["h2d_bytes"], t2["d2h_bytes"]
@@ -322,17 +329,28 @@ def run_gpu(args, rank, world):
                      "avg_launch_ms": avg_launch_s * 1e3,
                      "stage_ms_per_step": {k: v / args.steps for k, v in stage_ms.items()}})
 
-    # error of this form against the FP64 path on a strided subset
-    err = None
-    if args.fp64_check > 0 and prec == api.PREC_MIXED:
-        stride = max(1, (mp[0] * mp[1] * mp[2]) // args.fp64_check)
-        a = ctx.core_worker_loc(job, precision=api.PREC_MIXED, k_stride=stride)
+    # error of this form against the plain FP64 GPU path, and that path's throughput
+    err = fp64_path = None
+    if args.fp64_check != 0 and prec == api.PREC_MIXED:
+        if args.fp64_check < 0:
+            stride, a = ks, res
+        else:
+            stride = max(ks, (mp[0] * mp[1] * mp[2]) // args.fp64_check)
+            a = ctx.core_worker_loc(job, precision=api.PREC_MIXED, k_stride=stride)
+        ctx.core_worker_loc(job, precision=api.PREC_FP64, k_stride=stride, k_count=64 * 1024)   # builds its slabs
         b = ctx.core_worker_loc(job, precision=api.PREC_FP64, k_stride=stride)
+        t64 = ctx.timing()
+        fp64_path = {"value": b["n_k"] / (t64["run_ms"] * 1e-3), "unit": UNIT, "k_points": int(b["n_k"]),
+                     "ms": t64["run_ms"], "speedup_of_this_form": None}
         err = {"k_points": int(a["n_k"]), "k_stride": stride}
         for key in ("ahc", "mep_ic", "mep_lc", "mep_cs", "kubo_mep_ic", "kubo_mep_lc", "kubo_mep_cs"):
             x, y = np.asarray(a[key]), np.asarray(b[key])
             scale = float(np.abs(y).max())
             err[key] = float(np.abs(x - y).max() / scale) if scale > 0 else float(np.abs(x).max())
+        for key in ("velo_ahc", "kubo_ohc"):
+            if key in a and key in b:
+                x, y = np.asarray(a[key]), np.asarray(b[key])
+                err[key] = float(np.abs(x - y).max() / np.abs(y).max())
         # sigma_xy and the MEP tensor (sum over valence bands of IC + LC + CS)
         sxy = lambda r: r["ahc"][0, 1, 0]
         mep = lambda r: (np.asarray(r["mep_ic"]) + np.asarray(r["mep_lc"]) + np.asarray(r["mep_cs"])).sum(-1)
@@ -349,6 +367,8 @@ def run_gpu(args, rank, world):
         except Exception as exc:  # the baseline is reported, never required
             cpu = {"value": None, "unit": UNIT, "error": str(exc)}
 
+    if fp64_path is not None:
+        fp64_path["speedup_of_this_form"] = value / (world * fp64_path["value"])
     if rank == 0:
         out = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -369,6 +389,7 @@ def run_gpu(args, rank, world):
             "roofline": roofline,
             "cpu_baseline": cpu,
             "error_vs_fp64": err,
+            "fp64_path": fp64_path,
         }
         print(json.dumps(out))
 

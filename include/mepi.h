@@ -52,14 +52,17 @@ extern "C" {
 #define MEPI_OUT_AHC 1u
 #define MEPI_OUT_MEP_NIU 2u
 #define MEPI_OUT_KUBO_MEP 4u
+#define MEPI_OUT_OPT_HALL 8u    /* velo_ahc_tens + kubo_ohc_tens (src/kubo.f90:86-198),
+                                   which the reference computes with do_ahc
+                                   (src/core.f90:221-230); needs n_hw >= 1 */
 
 /* arithmetic form of the run */
 #define MEPI_PREC_FP64 0   /* all-FP64 plain form */
-#define MEPI_PREC_MIXED 1  /* split-FP16 tensor-core Fourier sums, FP32 per-k
-                              work, FP64 k-sums; k-points whose band gap falls
-                              below degen_gap, or whose occupation or kuboTol
-                              decisions lie within the FP32 error of their
-                              threshold, are rerun in FP64 */
+#define MEPI_PREC_MIXED 1  /* FP32 per-k work with FP64 H(k), compensated
+                              eigenpair refinement and velocity rotation, FP64
+                              energies for every decision and FP64 k-sums;
+                              k-points whose band gap falls below degen_gap
+                              are rerun in FP64 */
 
 typedef struct mepi_ctx mepi_ctx;
 
@@ -100,6 +103,10 @@ typedef struct {
     double degen_gap;          /* MEPI_PREC_MIXED only: minimum band gap (Ha)
                                   for the FP32 per-k path; < 0 = default
                                   (3e-3 Ha) */
+    int32_t n_hw;              /* MEPI_OUT_OPT_HALL: number of photon energies */
+    const double *hw_lst;      /* hw_lst(n_hw), Hartree ([Laser] get_linspace) */
+    double eta_smr;            /* [Fermi] eta_smearing, Hartree: the reference's
+                                  i_eta_smr = i * eta_smr */
 } mepi_job;
 
 /* Unnormalised local sums, like the reference's *_loc arrays
@@ -117,6 +124,10 @@ typedef struct {
     int64_t n_k_done;          /* n_ki_loc */
     int64_t n_k_fp64;          /* MEPI_PREC_MIXED: k-points rerun in FP64 */
     int32_t eig_max_sweeps;    /* largest Jacobi sweep count seen */
+    double *velo_ahc;          /* MEPI_OUT_OPT_HALL: velo_ahc_loc(3,3,n_hw,n_eF)
+                                  complex, as (re, im) pairs */
+    double *kubo_ohc;          /* MEPI_OUT_OPT_HALL: kubo_ohc_loc(3,3,n_hw,n_eF)
+                                  complex, as (re, im) pairs */
 } mepi_acc;
 
 /* Device time of each stage of the last mepi_run (CUDA events on the

@@ -30,7 +30,7 @@ LIB_PATH = os.path.join(HERE, "libmepi_gb300.so")
 
 OK, ERR_ARG, ERR_CUDA, ERR_NOMEM, ERR_EIG, ERR_NONHERM, ERR_NONFINITE = range(7)
 SEM_REF, SEM_PAPER = 0, 1
-OUT_AHC, OUT_MEP_NIU, OUT_KUBO_MEP = 1, 2, 4
+OUT_AHC, OUT_MEP_NIU, OUT_KUBO_MEP, OUT_OPT_HALL = 1, 2, 4, 8
 PREC_FP64, PREC_MIXED = 0, 1
 
 
@@ -52,14 +52,16 @@ class MepiJob(C.Structure):
     _fields_ = [("mp_grid", C.c_int32 * 3), ("k_begin", C.c_int64), ("k_stride", C.c_int64),
                 ("k_count", C.c_int64), ("n_eF", C.c_int32), ("ef_lst", C.c_void_p),
                 ("T_kelvin", C.c_double), ("valence_bands", C.c_int32), ("outputs", C.c_uint32),
-                ("precision", C.c_int32), ("chunk_k", C.c_int64), ("degen_gap", C.c_double)]
+                ("precision", C.c_int32), ("chunk_k", C.c_int64), ("degen_gap", C.c_double),
+                ("n_hw", C.c_int32), ("hw_lst", C.c_void_p), ("eta_smr", C.c_double)]
 
 
 class MepiAcc(C.Structure):
     _fields_ = [("Ne_sum", C.c_void_p), ("ahc", C.c_void_p),
                 ("mep_ic", C.c_void_p), ("mep_lc", C.c_void_p), ("mep_cs", C.c_void_p),
                 ("kubo_mep_ic", C.c_void_p), ("kubo_mep_lc", C.c_void_p), ("kubo_mep_cs", C.c_void_p),
-                ("n_k_done", C.c_int64), ("n_k_fp64", C.c_int64), ("eig_max_sweeps", C.c_int32)]
+                ("n_k_done", C.c_int64), ("n_k_fp64", C.c_int64), ("eig_max_sweeps", C.c_int32),
+                ("velo_ahc", C.c_void_p), ("kubo_ohc", C.c_void_p)]
 
 
 STAGES = ("ft", "phase", "fth", "eig", "refine", "rot", "gauge", "bandsum", "reduce")
@@ -180,8 +182,11 @@ class Context:
         """k-loop body of src/core.f90:165-270 for k = k_begin + s*k_stride.
 
         ``job`` keys: mp_grid, ef_lst (Hartree), T_kelvin, valence_bands and
-        optionally do_ahc / do_mep / do_kubo (default True).  Returns the
-        unnormalised local sums with the reference's shapes (Fortran order).
+        optionally do_ahc / do_mep / do_kubo (default True), and hw_lst
+        (Hartree) with eta_smr for the optical Hall tensors velo_ahc and
+        kubo_ohc (3,3,n_hw,n_eF) that the reference computes with do_ahc.
+        Returns the unnormalised local sums with the reference's shapes
+        (Fortran order).
         """
         ef = np.ascontiguousarray(np.atleast_1d(np.asarray(job["ef_lst"], np.float64)))
         nE = ef.size
@@ -200,6 +205,11 @@ class Context:
             outs |= OUT_MEP_NIU
         if job.get("do_kubo", True):
             outs |= OUT_KUBO_MEP
+        hw = job.get("hw_lst")
+        hw = None if hw is None else np.ascontiguousarray(np.atleast_1d(np.asarray(hw, np.float64)))
+        if (outs & OUT_AHC) and hw is not None and hw.size:
+            outs |= OUT_OPT_HALL
+            j.n_hw, j.hw_lst, j.eta_smr = hw.size, hw.ctypes.data, float(job.get("eta_smr", 0.0))
         j.outputs = outs
         j.precision = int(precision)
         j.chunk_k = int(chunk_k)
@@ -209,6 +219,9 @@ class Context:
                "mep_cs": np.zeros((3, 3, nv), order="F"),
                "kubo_mep_ic": np.zeros((3, 3, nE), order="F"), "kubo_mep_lc": np.zeros((3, 3, nE), order="F"),
                "kubo_mep_cs": np.zeros((3, 3, nE), order="F")}
+        if outs & OUT_OPT_HALL:
+            res["velo_ahc"] = np.zeros((3, 3, hw.size, nE), np.complex128, order="F")
+            res["kubo_ohc"] = np.zeros((3, 3, hw.size, nE), np.complex128, order="F")
         acc = MepiAcc()
         for key, arr in res.items():
             setattr(acc, key, arr.ctypes.data if arr.size else None)

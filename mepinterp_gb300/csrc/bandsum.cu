@@ -73,7 +73,7 @@ __global__ void __launch_bounds__(256) bandsum_kernel(DevModel md, JobDev jb, in
     T* Dt = Cs + kMaxN;                                           // [N][N] E_a - E_b (difference formed in FP64)
     T* Iv = Dt + NN;                                              // [N][N] 1 / (E_a - E_b), 0 on the diagonal
     const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nwarps = nt >> 5;
-    const AccLayout L{nE, nval};
+    const AccLayout L{nE, nval, jb.nW};
     double* P = partials + (size_t)blockIdx.x * L.size();
     const T ttol = (T)md.kubo_tol;
 
@@ -108,11 +108,16 @@ __global__ void __launch_bounds__(256) bandsum_kernel(DevModel md, JobDev jb, in
 
         for (int n0 = warp; n0 < N; n0 += nwarps) {
             const bool niu = (n0 < nval) && jb.do_mep;
+            // per-band curvature: FP64 in the FP64 form, double-FP32 (TwoSum) in
+            // the FP32 form, so that the pair terms of two occupied bands still
+            // cancel to well below the FP32 rounding of one term
             double s_curv[9];
+            DF s_curvf[9];
             T s_ic[9], s_lc[9], s_icv[9], s_lcv[9];
 #pragma unroll
             for (int q = 0; q < 9; ++q) {
                 s_curv[q] = 0.0;
+                s_curvf[q] = DF{0.f, 0.f};
                 s_ic[q] = s_lc[q] = s_icv[q] = s_lcv[q] = (T)0;
             }
             cplx<T> vnn[3];
@@ -138,7 +143,11 @@ __global__ void __launch_bounds__(256) bandsum_kernel(DevModel md, JobDev jb, in
 #pragma unroll
                     for (int j = 0; j < 3; ++j)
 #pragma unroll
-                        for (int i = 0; i < 3; ++i) s_curv[i + 3 * j] += (double)(w * (va[i] * vb[j]).im);
+                        for (int i = 0; i < 3; ++i) {
+                            const T term = w * (va[i] * vb[j]).im;
+                            if constexpr (sizeof(T) == 4) df_add(s_curvf[i + 3 * j], term);
+                            else s_curv[i + 3 * j] += (double)term;
+                        }
                 }
                 // LC
                 {
@@ -191,7 +200,13 @@ __global__ void __launch_bounds__(256) bandsum_kernel(DevModel md, JobDev jb, in
             }
 #pragma unroll
             for (int q = 0; q < 9; ++q) {
-                const double a = warp_sum(s_curv[q]);
+                double a;
+                if constexpr (sizeof(T) == 4) {
+                    const DF r = df_warp_sum(s_curvf[q]);
+                    a = (double)r.s + (double)r.c;
+                } else {
+                    a = warp_sum(s_curv[q]);
+                }
                 T b = warp_sum(s_ic[q]), c = warp_sum(s_lc[q]);
                 T d = warp_sum(s_icv[q]), e = warp_sum(s_lcv[q]);
                 if (lane == 0) {
@@ -285,6 +300,100 @@ __global__ void __launch_bounds__(256) bandsum_kernel(DevModel md, JobDev jb, in
     }
 }
 
+// Optical Hall tensors of one rank's k-points (the reference computes them
+// with do_ahc, src/core.f90:221-230), per ordered band pair n != m with
+// c_ij = V_i(n,m) V_j(m,n):
+//   velo_ahc_tens (src/kubo.f90:86-140)
+//       o(i,j,w,e) += (f(e,n) - f(e,m)) Im(c_ij) / ((E_n - E_m)^2 - (hw_w + i eta)^2)
+//   kubo_ohc_tens (src/kubo.f90:146-198), no degeneracy guard (D9)
+//       z(i,j,w,e) += i c_ij (f(e,m) - f(e,n)) / ((E_m - E_n)(E_m - E_n - hw_w - i eta))
+// Warp w takes the rows n = w, w + nwarps, ...; its lanes the columns m.  For
+// each (w, e) the per-row sums go to shared memory and are added over rows in
+// a fixed order into the CTA's FP64 slice, so the result is deterministic.
+// The band-energy differences entering the denominators are formed in FP64
+// (so that nothing cancels in T near a resonance E_n - E_m = +-hw); weights,
+// products and the per-row sums are in T, the sum over rows and k in FP64.
+template <typename T>
+__global__ void __launch_bounds__(256) opt_hall_kernel(DevModel md, JobDev jb, int64_t nk, const double* __restrict__ Eg,
+                                                       const cplx<T>* __restrict__ Vg, const int* __restrict__ skip,
+                                                       double* __restrict__ partials) {
+    extern __shared__ unsigned char smem_raw[];
+    const int N = md.N, NN = N * N, ld = N + 1;
+    cplx<T>* Vs = reinterpret_cast<cplx<T>*>(smem_raw);          // [3][N][ld]
+    double* rowacc = reinterpret_cast<double*>(Vs + 3 * N * ld);  // [N][36]
+    __shared__ double Es[kMaxN], fs[kMaxN];
+    const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nwarps = nt >> 5;
+    const AccLayout L{jb.nE, jb.nval, jb.nW};
+    double* P = partials + (size_t)blockIdx.x * L.size();
+    for (int64_t k = blockIdx.x; k < nk; k += gridDim.x) {
+        if (skip && skip[k]) continue;
+        __syncthreads();
+        for (int e = tid; e < 3 * NN; e += nt) {
+            const int a = e / NN, r = e % NN;
+            Vs[(a * N + r / N) * ld + r % N] = Vg[(size_t)k * 3 * NN + e];
+        }
+        for (int n = tid; n < N; n += nt) Es[n] = Eg[(size_t)k * N + n];
+        for (int e = 0; e < jb.nE; ++e) {
+            __syncthreads();
+            for (int n = tid; n < N; n += nt) fs[n] = fd_stat<double>(Es[n], jb.ef[e], jb.T_kelvin);
+            for (int w = 0; w < jb.nW; ++w) {
+                __syncthreads();
+                const double hw = jb.hw[w];
+                const T eta = (T)jb.eta;
+                for (int n = warp; n < N; n += nwarps) {
+                    T ov[18], oz[18];   // (re, im) of the 9 components
+#pragma unroll
+                    for (int q = 0; q < 18; ++q) ov[q] = oz[q] = (T)0;
+                    for (int m = lane; m < N; m += 32) {
+                        if (m == n) continue;
+                        // the differences in FP64, so that no cancellation near a
+                        // resonance (E_n - E_m = +-hw) is left to the working precision
+                        const double dnm = Es[n] - Es[m];
+                        const T dm = (T)(dnm - hw), dp = (T)(dnm + hw), d = (T)dnm, dh = (T)(-dnm - hw);
+                        // velo: (f_n - f_m) / ((E_n - E_m)^2 - (hw + i eta)^2)
+                        //     = (f_n - f_m) / ((d - hw)(d + hw) + eta^2 - 2 i hw eta)
+                        const T ar = dm * dp + eta * eta, ai = -(T)2 * (T)hw * eta;
+                        const T dfv = (T)(fs[n] - fs[m]);
+                        const T vin = dfv / (ar * ar + ai * ai);
+                        const T vr = ar * vin, vi = -ai * vin;
+                        // ohc: i (f_m - f_n) / ((E_m - E_n)(E_m - E_n - hw - i eta)),  E_m - E_n = -d
+                        const T br = -d * dh, bi = d * eta;
+                        const T dfo = (T)(fs[m] - fs[n]);
+                        const T oin = dfo / (br * br + bi * bi);
+                        const T orr = bi * oin, oi = br * oin;   // i (br - i bi) / |b|^2
+#pragma unroll
+                        for (int j = 0; j < 3; ++j)
+#pragma unroll
+                            for (int i = 0; i < 3; ++i) {
+                                const cplx<T> c = Vs[(i * N + n) * ld + m] * Vs[(j * N + m) * ld + n];
+                                const int q = 2 * (i + 3 * j);
+                                ov[q] += c.im * vr;
+                                ov[q + 1] += c.im * vi;
+                                oz[q] += c.re * orr - c.im * oi;
+                                oz[q + 1] += c.re * oi + c.im * orr;
+                            }
+                    }
+#pragma unroll
+                    for (int q = 0; q < 18; ++q) {
+                        const T a = warp_sum(ov[q]), b = warp_sum(oz[q]);
+                        if (lane == 0) {
+                            rowacc[n * 36 + q] = (double)a;
+                            rowacc[n * 36 + 18 + q] = (double)b;
+                        }
+                    }
+                }
+                __syncthreads();
+                for (int q = tid; q < 36; q += nt) {
+                    double acc = 0.0;
+                    for (int n = 0; n < N; ++n) acc += rowacc[n * 36 + q];
+                    const int base = q < 18 ? L.vah_off() : L.koh_off();
+                    P[base + (q % 18) + 18 * (w + jb.nW * e)] += acc;
+                }
+            }
+        }
+    }
+}
+
 __global__ void reduce_kernel(const double* __restrict__ partials, int n_cta, int size, double* __restrict__ out) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < size; i += gridDim.x * blockDim.x) {
         double s = 0.0;
@@ -316,10 +425,28 @@ cudaError_t launch_bandsum(const DevModel& m, const JobDev& j, int64_t nk, const
     const bool tables = bandsum_smem<T>(m.N, true) <= 227 * 1024;
     size_t smem = bandsum_smem<T>(m.N, tables);
     cudaError_t e = cudaFuncSetAttribute(bandsum_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(bandsum_kernel<T>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 cudaSharedmemCarveoutMaxShared);
     if (e != cudaSuccess) return e;
     bandsum_kernel<T><<<n_cta, 256, smem, s>>>(m, j, nk, E, V, CSV, skip, partials, tables ? 1 : 0);
     return cudaGetLastError();
 }
+
+template <typename T>
+cudaError_t launch_opt_hall(const DevModel& m, const JobDev& j, int64_t nk, const double* E, const cplx<T>* V,
+                            const int* skip, double* partials, int n_cta, cudaStream_t s) {
+    if (nk <= 0 || j.nW <= 0) return cudaSuccess;
+    const size_t smem = 3 * (size_t)m.N * (m.N + 1) * sizeof(cplx<T>) + (size_t)m.N * 36 * sizeof(double);
+    cudaError_t e = cudaFuncSetAttribute(opt_hall_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    opt_hall_kernel<T><<<n_cta, 256, smem, s>>>(m, j, nk, E, V, skip, partials);
+    return cudaGetLastError();
+}
+template cudaError_t launch_opt_hall<double>(const DevModel&, const JobDev&, int64_t, const double*,
+                                             const cplx<double>*, const int*, double*, int, cudaStream_t);
+template cudaError_t launch_opt_hall<float>(const DevModel&, const JobDev&, int64_t, const double*,
+                                            const cplx<float>*, const int*, double*, int, cudaStream_t);
 
 cudaError_t launch_reduce(const double* partials, int n_cta, int size, double* out, cudaStream_t s) {
     reduce_kernel<<<(size + 255) / 256, 256, 0, s>>>(partials, n_cta, size, out);

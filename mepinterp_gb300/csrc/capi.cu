@@ -204,9 +204,13 @@ int run_chunk(mepi_ctx* ctx, const KRange& kr, const JobDev* jb, int n_cta, doub
                                  ctx->OD.as<cplx<T>>(), ctx->stream)));
     STAGE(ST_GAUGE, (launch_gauge<T>(ctx->dm, nk, E64, ctx->HA.as<cplx<T>>(), ctx->OD.as<cplx<T>>(),
                                      ctx->V.as<cplx<T>>(), ctx->CSV.as<T>(), odh, ctx->stream)));
-    if (bandsum)
+    if (bandsum) {
         STAGE(ST_BAND, (launch_bandsum<T>(ctx->dm, *jb, nk, E64, ctx->V.as<cplx<T>>(), ctx->CSV.as<T>(), flags,
                                           ctx->partials.as<double>(), n_cta, ctx->stream)));
+        if (jb->nW > 0)
+            STAGE(ST_BAND, (launch_opt_hall<T>(ctx->dm, *jb, nk, E64, ctx->V.as<cplx<T>>(), flags,
+                                               ctx->partials.as<double>(), n_cta, ctx->stream)));
+    }
     return 0;
 }
 
@@ -306,10 +310,15 @@ int run_impl(mepi_ctx* ctx, const mepi_job* job, mepi_acc* out) {
     chunk = std::max<int64_t>(1, std::min<int64_t>(chunk, std::max<int64_t>(count, 1)));
     const double degen_gap = job->degen_gap >= 0 ? job->degen_gap : 3e-3;
 
-    AccLayout L{job->n_eF, job->valence_bands};
+    const bool opt_hall = (job->outputs & MEPI_OUT_OPT_HALL) != 0;
+    if (opt_hall && (job->n_hw <= 0 || !job->hw_lst || !finite_all(job->hw_lst, job->n_hw) ||
+                     !std::isfinite(job->eta_smr)))
+        return MEPI_ERR_ARG;
+    const int n_hw = opt_hall ? job->n_hw : 0;
+    AccLayout L{job->n_eF, job->valence_bands, n_hw};
     const int n_cta = bandsum_ctas();
     CKM(ctx->partials.ensure((size_t)n_cta * L.size() * sizeof(double)));
-    CKM(ctx->out.ensure((size_t)L.size() * sizeof(double) + (size_t)job->n_eF * sizeof(double)));
+    CKM(ctx->out.ensure((size_t)L.size() * sizeof(double) + (size_t)(job->n_eF + n_hw) * sizeof(double)));
     CKM(ctx->counters.ensure(4 * sizeof(int)));
     CK(cudaMemsetAsync(ctx->partials.p, 0, (size_t)n_cta * L.size() * sizeof(double), ctx->stream));
     CK(cudaMemsetAsync(ctx->counters.p, 0, 4 * sizeof(int), ctx->stream));
@@ -319,6 +328,11 @@ int run_impl(mepi_ctx* ctx, const mepi_job* job, mepi_acc* out) {
     double* d_ef = ctx->out.as<double>() + L.size();
     CK(cudaMemcpyAsync(d_ef, job->ef_lst, job->n_eF * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
     ctx->h2d += job->n_eF * sizeof(double);
+    double* d_hw = d_ef + job->n_eF;
+    if (n_hw) {
+        CK(cudaMemcpyAsync(d_hw, job->hw_lst, n_hw * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+        ctx->h2d += n_hw * sizeof(double);
+    }
     JobDev jb;
     jb.nE = job->n_eF;
     jb.nval = job->valence_bands;
@@ -327,6 +341,9 @@ int run_impl(mepi_ctx* ctx, const mepi_job* job, mepi_acc* out) {
     jb.do_kubo = (job->outputs & MEPI_OUT_KUBO_MEP) ? 1 : 0;
     jb.T_kelvin = job->T_kelvin;
     jb.ef = d_ef;
+    jb.nW = n_hw;
+    jb.hw = n_hw ? d_hw : nullptr;
+    jb.eta = job->eta_smr;
 
     std::vector<int64_t> redo;
     int rc = 0;
@@ -415,6 +432,10 @@ int run_impl(mepi_ctx* ctx, const mepi_job* job, mepi_acc* out) {
     put(out->mep_ic, L.mic_off(), 9 * nv);
     put(out->mep_lc, L.mlc_off(), 9 * nv);
     put(out->mep_cs, L.mcs_off(), 9 * nv);
+    if (n_hw) {
+        put(out->velo_ahc, L.vah_off(), 18 * n_hw * nE);
+        put(out->kubo_ohc, L.koh_off(), 18 * n_hw * nE);
+    }
     out->n_k_done = count;
     out->n_k_fp64 = fp64 ? count : (int64_t)redo.size();
     out->eig_max_sweeps = hc[0];

@@ -284,6 +284,8 @@ cudaError_t launch_eig(int N, int64_t nk, const cplx<T>* W, int nbW, const cplx<
     auto go = [&](auto kern, int NP, int threads) {
         const size_t smem = 6 * (size_t)NP * (NP + 1) * sizeof(T);
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
         if (e != cudaSuccess) return e;
         kern<<<grid, threads, smem, s>>>(N, nk, kblock, W, nbW, H64, E, U, max_sweeps, sweeps_max, flag_cap, degen_gap,
                                          redo_flag);
@@ -325,9 +327,10 @@ __global__ void __launch_bounds__(256) refine_kernel(int N, const cplx<double>* 
     const int Np = N + (N & 1), NPP = Np * Np, h = Np / 2;
     double* rho = reinterpret_cast<double*>(smem_raw);
     double* En = rho + Np;
-    double* Sn = En + Np;
-    double* Dn = Sn + Np;
-    cplx<float>* Hh = reinterpret_cast<cplx<float>*>(Dn + Np);
+    float* Sn = reinterpret_cast<float*>(En + Np);
+    float* Dn = Sn + Np;
+    float* Iv = Dn + Np;                       // [Np][Np] inverse gaps
+    cplx<float>* Hh = reinterpret_cast<cplx<float>*>(Iv + NPP);
     cplx<float>* Hl = Hh + NPP;
     cplx<float>* Us = Hl + NPP;
     cplx<float>* Rs = Us + NPP;
@@ -401,61 +404,54 @@ __global__ void __launch_bounds__(256) refine_kernel(int N, const cplx<double>* 
     // P = U^dag R (FP32)
     smem_cgemm<float, true>(Np, Np, Us, Rs, Ps, tid, nt);
     for (int n = tid; n < N; n += nt) {
-        double sq = 0.0;
-        for (int l = 0; l < N; ++l) {
-            const cplx<float> u = Us[l * Np + n];
-            sq += (double)u.re * u.re + (double)u.im * u.im;
-        }
+        float sq = 0.f;   // |u_n|^2 = 1 + O(1e-5): FP32 keeps P_nn / S_nn to ~1e-13
+        for (int l = 0; l < N; ++l) sq += abs2(Us[l * Np + n]);
         Sn[n] = sq;
     }
     __syncthreads();
     for (int n = tid; n < N; n += nt) rho[n] = (double)ls[n] + (double)Ps[n * Np + n].re / Sn[n];
     __syncthreads();
-    for (int n = tid; n < N; n += nt) {
-        double e2 = rho[n];
-        bool bad = !isfinite(e2);
-        for (int m = 0; m < N; ++m) {
-            if (m == n) continue;
+    // inverse gaps 1 / (rho_n - rho_m): the degeneracy decision on the FP64
+    // difference, the reciprocal in FP32 (it scales corrections of order |P|/gap)
+    for (int e = tid; e < NPP; e += nt) {
+        const int m = e / Np, n = e % Np;
+        float iv = 0.f;
+        if (m < N && n < N && m != n) {
             const double d = rho[n] - rho[m];
-            if (!(fabs(d) > degen_gap)) { bad = true; continue; }
-            const cplx<float> p = Ps[m * Np + n];
-            e2 += ((double)p.re * p.re + (double)p.im * p.im) / d;
+            if (fabs(d) > degen_gap) iv = 1.f / (float)d;
+            else s_flag = 1;
         }
-        En[n] = e2;
-        if (bad || !isfinite(e2)) s_flag = 1;
+        Iv[e] = iv;
+    }
+    __syncthreads();
+    for (int n = tid; n < N; n += nt) {
+        float e2 = 0.f;
+        for (int m = 0; m < N; ++m) e2 += abs2(Ps[m * Np + n]) * Iv[m * Np + n];
+        const double en = rho[n] + (double)e2;
+        En[n] = en;
+        if (!isfinite(en)) s_flag = 1;
     }
     __syncthreads();
     // C1 into Rs; X (P without its diagonal) stays in Ps
     for (int e = tid; e < NPP; e += nt) {
         const int m = e / Np, n = e % Np;
-        cplx<float> c = mk(0.f, 0.f);
-        if (m < N && n < N && m != n) {
-            const double d = rho[n] - rho[m];
-            if (fabs(d) > degen_gap) c = mk((float)((double)Ps[e].re / d), (float)((double)Ps[e].im / d));
-        }
-        Rs[e] = c;
+        Rs[e] = Iv[e] * Ps[e];
         if (m == n) Ps[e] = mk(0.f, 0.f);
     }
     __syncthreads();
     // X C1 into Hh (H is no longer needed); diagonal of the normalisation term
     smem_cgemm<float, false>(Np, Np, Ps, Rs, Hh, tid, nt);
     for (int n = tid; n < Np; n += nt) {
-        double q = 0.0;
-        for (int m = 0; m < N; ++m) q += (double)abs2(Rs[m * Np + n]);
-        Dn[n] = -0.5 * q;
+        float q = 0.f;
+        for (int m = 0; m < N; ++m) q += abs2(Rs[m * Np + n]);
+        Dn[n] = -0.5f * q;
     }
     __syncthreads();
     // C = C1 + C2 into Rs
     for (int e = tid; e < NPP; e += nt) {
         const int m = e / Np, n = e % Np;
         if (m >= N || n >= N) continue;
-        if (m == n) {
-            Rs[e] = mk((float)Dn[n], 0.f);
-        } else {
-            const double d = rho[n] - rho[m];
-            if (fabs(d) > degen_gap)
-                Rs[e] = Rs[e] + mk((float)((double)Hh[e].re / d), (float)((double)Hh[e].im / d));
-        }
+        Rs[e] = (m == n) ? mk(Dn[n], 0.f) : Rs[e] + Iv[e] * Hh[e];
     }
     __syncthreads();
     // U C into Ps
@@ -478,7 +474,8 @@ __global__ void __launch_bounds__(256) refine_kernel(int N, const cplx<double>* 
 
 size_t refine_smem_bytes(int N) {
     const size_t Np = N + (N & 1);
-    return 4 * Np * sizeof(double) + 5 * Np * Np * sizeof(cplx<float>);
+    return 2 * Np * sizeof(double) + 2 * Np * sizeof(float) + Np * Np * sizeof(float) +
+           5 * Np * Np * sizeof(cplx<float>);
 }
 
 cudaError_t launch_refine(int N, int64_t nk, const cplx<double>* H64, const float* lam, cplx<float>* U, double* E64,
@@ -486,6 +483,9 @@ cudaError_t launch_refine(int N, int64_t nk, const cplx<double>* H64, const floa
     if (nk <= 0) return cudaSuccess;
     const size_t smem = refine_smem_bytes(N);
     cudaError_t e = cudaFuncSetAttribute(refine_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(refine_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 cudaSharedmemCarveoutMaxShared);
     if (e != cudaSuccess) return e;
     refine_kernel<<<(unsigned)nk, N <= 16 ? 128 : 256, smem, s>>>(N, H64, lam, U, E64, degen_gap, redo_flag);
     return cudaGetLastError();

@@ -72,18 +72,6 @@ __global__ void sep_stage_b(const cplx<double>* __restrict__ G1, cplx<double>* _
     }
 }
 
-// Upper-triangle element u (row-major over n <= m) -> (n, m).  Row n holds
-// N - n elements and starts at off(n) = n (2N - n + 1) / 2.
-__device__ __forceinline__ void upper_pair(int u, int N, int& n, int& mm) {
-    const float b = 2.f * N + 1.f;
-    int r = (int)((b - sqrtf(b * b - 8.f * u)) * 0.5f);
-    r = r < 0 ? 0 : (r > N - 1 ? N - 1 : r);
-    while (r > 0 && r * (2 * N - r + 1) / 2 > u) --r;
-    while (r < N - 1 && (r + 1) * (2 * N - r) / 2 <= u) ++r;
-    n = r;
-    mm = r + (u - r * (2 * N - r + 1) / 2);
-}
-
 __device__ __forceinline__ void item_coords(const KRange& kr, int64_t i, int q[3], double k[3]) {
     const int64_t ki = k_of(kr, i);
     q[0] = (int)(ki % kr.mp[0]);

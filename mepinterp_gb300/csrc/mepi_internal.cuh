@@ -94,6 +94,55 @@ __device__ __forceinline__ void smem_cgemm(int N, int ld, const cplx<T>* __restr
     }
 }
 
+// Upper-triangle element u (row-major over n <= m) -> (n, m).  Row n holds
+// N - n elements and starts at off(n) = n (2N - n + 1) / 2.
+__device__ __forceinline__ void upper_pair(int u, int N, int& n, int& mm) {
+    const float b = 2.f * N + 1.f;
+    int r = (int)((b - sqrtf(b * b - 8.f * u)) * 0.5f);
+    r = r < 0 ? 0 : (r > N - 1 ? N - 1 : r);
+    while (r > 0 && r * (2 * N - r + 1) / 2 > u) --r;
+    while (r < N - 1 && (r + 1) * (2 * N - r) / 2 <= u) ++r;
+    n = r;
+    mm = r + (u - r * (2 * N - r + 1) / 2);
+}
+
+// C = A^dag B known to be Hermitian (A, B complex Np x Np in shared memory,
+// row stride ld, Np even): only the 2 x 2 tiles on or above the diagonal are
+// formed, walked compactly so that whole warps drop out, and the strictly
+// upper elements are mirrored.
+template <typename T>
+__device__ __forceinline__ void smem_cgemm_herm(int Np, int ld, const cplx<T>* __restrict__ A,
+                                                const cplx<T>* __restrict__ B, cplx<T>* __restrict__ Cm, int tid,
+                                                int nt) {
+    const int h = Np >> 1;
+    for (int u = tid; u < h * (h + 1) / 2; u += nt) {
+        int a, b;
+        upper_pair(u, h, a, b);
+        const int i0 = 2 * a, j0 = 2 * b;
+        cplx<T> c00 = mk((T)0, (T)0), c01 = c00, c10 = c00, c11 = c00;
+        for (int l = 0; l < Np; ++l) {
+            const cplx<T> a0 = conjg(A[l * ld + i0]), a1 = conjg(A[l * ld + i0 + 1]);
+            const cplx<T> b0 = B[l * ld + j0], b1 = B[l * ld + j0 + 1];
+            fma_c(c00, a0, b0);
+            fma_c(c01, a0, b1);
+            fma_c(c10, a1, b0);
+            fma_c(c11, a1, b1);
+        }
+        Cm[i0 * ld + j0] = c00;
+        Cm[i0 * ld + j0 + 1] = c01;
+        Cm[(i0 + 1) * ld + j0 + 1] = c11;
+        if (i0 == j0) {
+            Cm[(i0 + 1) * ld + j0] = conjg(c01);
+        } else {
+            Cm[(i0 + 1) * ld + j0] = c10;
+            Cm[j0 * ld + i0] = conjg(c00);
+            Cm[(j0 + 1) * ld + i0] = conjg(c01);
+            Cm[j0 * ld + i0 + 1] = conjg(c10);
+            Cm[(j0 + 1) * ld + i0 + 1] = conjg(c11);
+        }
+    }
+}
+
 // Compensated FP32 arithmetic (Knuth's TwoSum, TwoProduct by FMA, and the
 // Dot2 summation of Ogita, Rump and Oishi, SIAM J. Sci. Comput. 26 (2005)):
 // a dot product of FP32 numbers accumulated as an unevaluated sum s + c, as if
@@ -102,6 +151,29 @@ __device__ __forceinline__ void smem_cgemm(int N, int ld, const cplx<T>* __restr
 struct DF {
     float s, c;
 };
+// acc += x (TwoSum: the rounding error of the leading sum goes to acc.c)
+__device__ __forceinline__ void df_add(DF& acc, float x) {
+    const float t = __fadd_rn(acc.s, x);
+    const float bp = __fsub_rn(t, acc.s);
+    const float e = __fadd_rn(__fsub_rn(acc.s, __fsub_rn(t, bp)), __fsub_rn(x, bp));
+    acc.s = t;
+    acc.c = __fadd_rn(acc.c, e);
+}
+// a + b of two unevaluated sums
+__device__ __forceinline__ DF df_sum(DF a, DF b) {
+    DF r{a.s, __fadd_rn(a.c, b.c)};
+    df_add(r, b.s);
+    return r;
+}
+// sum over the 32 lanes of a warp, in double-FP32
+__device__ __forceinline__ DF df_warp_sum(DF v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const DF w{__shfl_xor_sync(0xffffffffu, v.s, o), __shfl_xor_sync(0xffffffffu, v.c, o)};
+        v = df_sum(v, w);
+    }
+    return v;
+}
 __device__ __forceinline__ void df_add_prod(DF& acc, float a, float b) {
     const float p = __fmul_rn(a, b);
     const float pe = __fmaf_rn(a, b, -p);          // a b = p + pe exactly
@@ -117,18 +189,22 @@ __device__ __forceinline__ void df_add_prod(DF& acc, float a, float b) {
 // twice the working precision; 2 x 2 output tiles per thread.  op(A) = A^dag
 // when adjA.  Blo (optional) is a low-order part of B, added in plain FP32.
 // Chi receives the rounded result; Clo (optional) the remainder
-// (C = Chi + Clo to about 2^-44 relative).  With upper, only tiles with
-// i0 <= j0 are formed and the Hermitian mirror of the strictly upper ones is
-// written (for products known to be Hermitian).
+// (C = Chi + Clo to about 2^-44 relative).  With upper, only the tiles on or
+// above the diagonal are formed (walked compactly, so that whole warps drop
+// out) and the Hermitian mirror of the strictly upper elements is written (for
+// products known to be Hermitian).
 template <bool adjA>
 __device__ __forceinline__ void cgemm_dot2(int Np, int ld, const cplx<float>* __restrict__ A,
                                            const cplx<float>* __restrict__ B, const cplx<float>* __restrict__ Blo,
                                            cplx<float>* __restrict__ Chi, cplx<float>* __restrict__ Clo, bool upper,
                                            int tid, int nt) {
     const int h = Np >> 1;
-    for (int t = tid; t < h * h; t += nt) {
-        const int i0 = 2 * (t / h), j0 = 2 * (t % h);
-        if (upper && i0 > j0) continue;
+    const int ntile = upper ? h * (h + 1) / 2 : h * h;
+    for (int t = tid; t < ntile; t += nt) {
+        int a, b;
+        if (upper) upper_pair(t, h, a, b);
+        else { a = t / h; b = t % h; }
+        const int i0 = 2 * a, j0 = 2 * b;
         DF re[2][2], im[2][2];
         cplx<float> lo[2][2];
 #pragma unroll
@@ -276,11 +352,14 @@ struct JobDev {
     int nE, nval, do_ahc, do_mep, do_kubo;
     double T_kelvin;
     const double* ef;         // device (nE)
+    int nW = 0;               // photon energies of the optical Hall tensors (0 = off)
+    const double* hw = nullptr;   // device (nW)
+    double eta = 0.0;
 };
 
 // Layout of one CTA's FP64 accumulator slice.
 struct AccLayout {
-    int nE, nval;
+    int nE, nval, nW = 0;
     __host__ __device__ int ne_off() const { return 0; }
     __host__ __device__ int ahc_off() const { return nE; }
     __host__ __device__ int kic_off() const { return nE + 9 * nE; }
@@ -289,7 +368,10 @@ struct AccLayout {
     __host__ __device__ int mic_off() const { return nE + 36 * nE; }
     __host__ __device__ int mlc_off() const { return nE + 36 * nE + 9 * nval; }
     __host__ __device__ int mcs_off() const { return nE + 36 * nE + 18 * nval; }
-    __host__ __device__ int size() const { return nE + 36 * nE + 27 * nval; }
+    // velo_ahc and kubo_ohc: (3,3,nW,nE) complex as (re, im) pairs
+    __host__ __device__ int vah_off() const { return nE + 36 * nE + 27 * nval; }
+    __host__ __device__ int koh_off() const { return vah_off() + 18 * nW * nE; }
+    __host__ __device__ int size() const { return nE + 36 * nE + 27 * nval + 36 * nW * nE; }
 };
 
 // ---- host launchers (one per translation unit) ----
@@ -312,6 +394,9 @@ template <typename T>
 cudaError_t launch_bandsum(const DevModel& m, const JobDev& j, int64_t nk, const double* E, const cplx<T>* V,
                            const T* CSV, const int* skip, double* partials, int n_cta, cudaStream_t s);
 cudaError_t launch_reduce(const double* partials, int n_cta, int size, double* out, cudaStream_t s);
+template <typename T>
+cudaError_t launch_opt_hall(const DevModel& m, const JobDev& j, int64_t nk, const double* E, const cplx<T>* V,
+                            const int* skip, double* partials, int n_cta, cudaStream_t s);
 
 // Separable Fourier sums on a Monkhorst-Pack mesh (ft_sep.cu).  The slabs
 // G2[qx][qy][iz][blk][pair] stay resident in HBM for the run.

@@ -94,7 +94,7 @@ __global__ void __launch_bounds__(256) rot_kernel(DevModel m, const cplx<T>* __r
         }
         smem_cgemm<T, false>(Np, ld, Xs, Us, Ts, tid, nt);          // T = X U
         __syncthreads();
-        smem_cgemm<T, true>(Np, ld, Us, Ts, Xs, tid, nt);           // Y = U^dag T (into Xs)
+        smem_cgemm_herm<T>(Np, ld, Us, Ts, Xs, tid, nt);            // Y = U^dag T (Hermitian, into Xs)
         __syncthreads();
         for (int e = tid; e < NN; e += nt) HAk[(size_t)j * NN + e] = Xs[(e / N) * ld + e % N];
     }
@@ -123,6 +123,9 @@ cudaError_t launch_rot(const DevModel& m, int64_t nk, const cplx<T>* W, const cp
     const int Np = m.N + (m.N & 1);
     size_t smem = (sizeof(T) == 4 ? 4 : 3) * (size_t)Np * (Np + 1) * sizeof(cplx<T>);
     cudaError_t e = cudaFuncSetAttribute(rot_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(rot_kernel<T>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 cudaSharedmemCarveoutMaxShared);
     if (e != cudaSuccess) return e;
     int threads = m.N <= 16 ? 128 : 256;
     rot_kernel<T><<<(unsigned)nk, threads, smem, s>>>(m, W, U, HA, OD);

@@ -123,6 +123,9 @@ def random_tb_model(n_wf: int = 8, r_max: int = 1, decay: float = 1.0, seed: int
 
 
 # Workloads: the model, mesh and Fermi settings each benchmark configuration uses.
+# Every workload runs the reference's AHE job in full: with do_ahc it also forms
+# velo_ahc_tens and kubo_ohc_tens (src/core.f90:221-230), here at one photon
+# energy hw = 0 with the 1 meV broadening of the plain configuration.
 WORKLOADS = {
     # plain FP64 case: nWf=8, R in {-1,0,1}^3, 16^3 mesh, E_F = 0, T = 0
     "tb8_r1_k16": dict(model=dict(n_wf=8, r_max=1, decay=1.0, seed=1), mp_grid=(16, 16, 16),
@@ -141,5 +144,7 @@ def workload(name: str):
     w = WORKLOADS[name]
     model = random_tb_model(**w["model"])
     job = dict(mp_grid=tuple(w["mp_grid"]), ef_lst=np.asarray(w["ef_ev"], np.float64) / AU_TO_EV,
-               T_kelvin=float(w["T_kelvin"]), valence_bands=int(w["valence_bands"]))
+               T_kelvin=float(w["T_kelvin"]), valence_bands=int(w["valence_bands"]),
+               hw_lst=np.asarray(w.get("hw_ev", [0.0]), np.float64) / AU_TO_EV,
+               eta_smr=float(w.get("eta_ev", 1e-3)) / AU_TO_EV)
     return model, job

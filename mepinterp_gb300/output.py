@@ -8,7 +8,9 @@ integrate_over_k_space  src/core.f90:419-561 (+ mep_sum_bands :570-603) -- sums
                         the Niu MEP over valence bands, keeps only the selected
                         E_F slice of the Kubo tensors (D10) and divides by
                         |V_cell| N_k (normalize_k_int, src/k_space.f90:81-202).
-write_outputs           the file names of src/file_io.f90:238-359, written with
+write_outputs           the file names of src/file_io.f90:186-359 (with
+                        ahcVELO.npy / ohcVELO.npy of velo_ahc_tens and
+                        kubo_ohc_tens, and hw_lst.npy), written with
                         Fortran ordering as NPY-for-Fortran does; additionally
                         the full Fermi sweeps (*_sweep.npy), which the
                         reference accumulates but does not write.
@@ -55,11 +57,14 @@ def integrate_over_k_space(loc: dict, mp_grid, a_latt, valence_bands: int, n_k_g
     out["kubo_mep_tens"] = out["kubo_mep_ic"] + out["kubo_mep_lc"] + out["kubo_mep_cs"]
     out["ahc_tens"] = np.asarray(loc["ahc"])[:, :, e] / norm
     out["ahc_sweep"] = np.asarray(loc["ahc"]) / norm
+    if "velo_ahc" in loc:                      # src/core.f90:501-508: the selected E_F slice
+        out["ahc_velo"] = np.asarray(loc["velo_ahc"])[:, :, :, e] / norm
+        out["ohc_velo"] = np.asarray(loc["kubo_ohc"])[:, :, :, e] / norm
     return out
 
 
 def write_outputs(out_dir: str, res: dict, ef_lst, do_mep=True, do_kubo=True, do_ahc=True,
-                  write_mep_bands=True) -> list:
+                  write_mep_bands=True, hw_lst=None) -> list:
     os.makedirs(out_dir, exist_ok=True)
     written = []
 
@@ -81,7 +86,12 @@ def write_outputs(out_dir: str, res: dict, ef_lst, do_mep=True, do_kubo=True, do
             save(k + ".npy", res[k])
         for k in ("kubo_mep_ic", "kubo_mep_lc", "kubo_mep_cs"):
             save(k + "_sweep.npy", res[k + "_sweep"])
+    if hw_lst is not None and len(hw_lst) > 1:   # write_hw_list, src/file_io.f90:186-214 (eV)
+        save("hw_lst.npy", np.asarray(hw_lst, np.float64) * AU_TO_EV)
     if do_ahc:
         save("ahc_tens.npy", res["ahc_tens"])
         save("ahc_sweep.npy", res["ahc_sweep"])
+        if "ahc_velo" in res:                  # write_ahc_tensor, src/file_io.f90:340-359
+            save("ahcVELO.npy", res["ahc_velo"])
+            save("ohcVELO.npy", res["ohc_velo"])
     return written

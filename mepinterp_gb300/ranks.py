@@ -29,11 +29,16 @@ def reduce_loc(loc: dict, group=None) -> dict:
     import torch
     import torch.distributed as dist
     out = {}
-    for k in LOC_KEYS:
-        a = np.asarray(loc[k], dtype=np.float64)
-        t = torch.from_numpy(np.ascontiguousarray(a.ravel(order="F")).copy())
+    for k in LOC_KEYS + tuple(x for x in ("velo_ahc", "kubo_ohc") if x in loc):
+        a = np.asarray(loc[k])
+        cplx = np.iscomplexobj(a)
+        flat = a.ravel(order="F")
+        flat = np.stack([flat.real, flat.imag], axis=1).ravel() if cplx else flat.astype(np.float64)
+        t = torch.from_numpy(np.ascontiguousarray(flat).copy())
         dist.all_reduce(t, op=dist.ReduceOp.SUM, group=group)
-        out[k] = t.numpy().reshape(a.shape, order="F")
+        r = t.numpy()
+        r = r[0::2] + 1j * r[1::2] if cplx else r
+        out[k] = r.reshape(a.shape, order="F")
     n = torch.tensor([int(loc["n_k"])], dtype=torch.int64)
     dist.all_reduce(n, op=dist.ReduceOp.SUM, group=group)
     out["n_k"] = int(n.item())

@@ -151,11 +151,13 @@ def write_r_file(path: str, model: TBModel, header: str = "position operator") -
 def write_input_cfg(path: str, *, seed_name: str, a_latt: np.ndarray, mp_grid, valence_bands: int,
                     wf_centers: Optional[np.ndarray] = None, eF_min=0.0, eF_max=0.0, N_eF=1, Tkelvin=0.0,
                     eta_smearing=0.1, kubo_tol=1e-5, do_mep=True, do_kubo=True, do_ahc=True,
-                    do_gauge_trafo=True, use_cart_velo=False, n_hw=1, hw_min=0.0, hw_max=0.0) -> None:
+                    do_gauge_trafo=True, use_cart_velo=False, n_hw=1, hw_min=0.0, hw_max=0.0,
+                    plot_bands=False, do_write_velo=False) -> None:
     """input.cfg with the sections of scripts/tb_input_writer.py:102-190."""
     a = np.asarray(a_latt, np.float64)
     T = lambda b: "T" if b else "F"
-    lines = ["[jobs]", "    plot_bands=F", "    debug_mode=F", "    R_vect_float=F", "    do_write_velo=F",
+    lines = ["[jobs]", f"    plot_bands={T(plot_bands)}", "    debug_mode=F", "    R_vect_float=F",
+             f"    do_write_velo={T(do_write_velo)}",
              f"    do_mep={T(do_mep)}", f"    do_kubo={T(do_kubo)}", f"    do_ahc={T(do_ahc)}", "    do_opt=F",
              "    do_gyro=F", "", "[unitCell]"]
     for i in range(3):
@@ -176,6 +178,13 @@ def write_input_cfg(path: str, *, seed_name: str, a_latt: np.ndarray, mp_grid, v
               f"    N_hw= {n_hw}", f"    hw_min= {float(hw_min)!r}", f"    hw_max= {float(hw_max)!r}", ""]
     with open(path, "w") as out:
         out.write("\n".join(lines))
+
+
+def _linspace(lo: float, hi: float, n: int) -> np.ndarray:
+    """get_linspace, src/matrix_math.f90:74-100: n points from lo to hi, or [lo]."""
+    if n > 1:
+        return np.array([lo + i * (hi - lo) / (n - 1) for i in range(n)])
+    return np.array([lo])
 
 
 def _flag(v: str) -> bool:
@@ -211,8 +220,7 @@ def read_input_cfg(path: str) -> dict:
     n_ef = int(get("Fermi", "N_eF", "1"))
     ef_min = float(get("Fermi", "eF_min", "0")) / AU_TO_EV
     ef_max = float(get("Fermi", "eF_max", "0")) / AU_TO_EV
-    ef_lst = np.array([ef_min + i * (ef_max - ef_min) / (n_ef - 1) for i in range(n_ef)]) if n_ef > 1 \
-        else np.array([ef_min])  # get_linspace, src/matrix_math.f90:74-100
+    ef_lst = _linspace(ef_min, ef_max, n_ef)
     return {
         "seed_name": get("wannBase", "seed_name", "wf1").strip(),
         "a_latt": a_latt, "wf_centers": tau,
@@ -226,4 +234,8 @@ def read_input_cfg(path: str) -> dict:
         "do_write_mep_bands": _flag(get("MEP", "do_write_mep_bands", "F")),
         "do_mep": _flag(get("jobs", "do_mep", "F")), "do_kubo": _flag(get("jobs", "do_kubo", "F")),
         "do_ahc": _flag(get("jobs", "do_ahc", "F")),
+        "hw_lst": _linspace(float(get("Laser", "hw_min", "0")) / AU_TO_EV, float(get("Laser", "hw_max", "0")) / AU_TO_EV,
+                            int(get("Laser", "N_hw", "1"))),
+        "plot_bands": _flag(get("jobs", "plot_bands", "F")),
+        "do_write_velo": _flag(get("jobs", "do_write_velo", "F")),
     }

@@ -16,6 +16,8 @@
  *   get_velo ............ src/wann_interp.f90:406-444
  *   fd_stat / N_el ...... src/statistics.f90:41-124
  *   kubo_ahc_tens ....... src/kubo.f90:37-78
+ *   velo_ahc_tens,
+ *   kubo_ohc_tens ....... src/kubo.f90:86-198
  *   mep_niu_* ........... src/mep_niu.f90:20-159
  *   kubo_mep_* .......... src/kubo_mep.f90:16-149
  * with the same documented positions on D1 (A_bar = U^dag A U), D2
@@ -62,6 +64,9 @@ typedef struct {
     double T_kelvin;
     int32_t valence_bands;
     int32_t do_ahc, do_mep, do_kubo;
+    int32_t n_hw;             /* 0: no optical Hall tensors */
+    const double *hw_lst;     /* (n_hw) Hartree */
+    double eta_smr;           /* smearing: the reference's i_eta_smr = i * eta */
 } oracle_job;
 
 typedef struct {
@@ -70,6 +75,7 @@ typedef struct {
     double *mep_ic, *mep_lc, *mep_cs;                /* (3,3,n_val) */
     double *kubo_mep_ic, *kubo_mep_lc, *kubo_mep_cs; /* (3,3,n_eF) */
     int64_t n_k;
+    double *velo_ahc, *kubo_ohc;  /* (3,3,n_hw,n_eF) complex interleaved, or NULL */
 } oracle_out;
 
 static zheevd_fn g_zheevd = 0;
@@ -342,7 +348,7 @@ static int interp_k(const oracle_model *md, const double kpt[3], ws_t *w, zc *Ab
 
 /* band sums for one k, added into the given accumulators */
 static void band_sums(const oracle_model *md, const oracle_job *jb, ws_t *w, double *Ne, double *ahc,
-                      double *mic, double *mlc, double *mcs, double *kic, double *klc, double *kcs) {
+                      double *mic, double *mlc, double *mcs, double *kic, double *klc, double *kcs, zc *vah, zc *koh) {
     const int N = w->N, nE = jb->n_eF, nv = jb->valence_bands;
     const double tol = md->kubo_tol;
     const zc *V = w->V;
@@ -464,6 +470,43 @@ static void band_sums(const oracle_model *md, const oracle_job *jb, ws_t *w, dou
             for (int e = 0; e < nE; ++e)
                 for (int q = 0; q < 9; ++q) ahc[q + 9 * e] -= curv[q] * w->fd[e + nE * n];
         }
+        if (jb->n_hw > 0 && jb->hw_lst) {
+            const int nW = jb->n_hw;
+            const zc ieta = I * jb->eta_smr;
+            /* velo_ahc_tens (src/kubo.f90:86-140) */
+            for (int n = 0; n < N; ++n)
+                for (int np = 0; np < N; ++np) {
+                    if (np == n) continue;
+                    const double dE2 = (E[n] - E[np]) * (E[n] - E[np]);
+                    double v[9];
+                    for (int j = 0; j < 3; ++j)
+                        for (int i = 0; i < 3; ++i) v[i + 3 * j] = cimag(V[IXA(i, n, np, N)] * V[IXA(j, np, n, N)]);
+                    for (int h = 0; h < nW; ++h) {
+                        const zc z = jb->hw_lst[h] + ieta;
+                        const zc den = dE2 - z * z;
+                        for (int e = 0; e < nE; ++e) {
+                            const double df = w->fd[e + nE * n] - w->fd[e + nE * np];
+                            for (int q = 0; q < 9; ++q) vah[q + 9 * (h + (size_t)nW * e)] += df * v[q] / den;
+                        }
+                    }
+                }
+            /* kubo_ohc_tens (src/kubo.f90:146-198), no degeneracy guard (D9) */
+            for (int m = 0; m < N; ++m)
+                for (int n = 0; n < N; ++n) {
+                    if (m == n) continue;
+                    const double dE = E[m] - E[n];
+                    zc v[9];
+                    for (int j = 0; j < 3; ++j)
+                        for (int i = 0; i < 3; ++i) v[i + 3 * j] = V[IXA(i, n, m, N)] * V[IXA(j, m, n, N)];
+                    for (int h = 0; h < nW; ++h) {
+                        const zc den = dE * (dE - jb->hw_lst[h] - ieta);
+                        for (int e = 0; e < nE; ++e) {
+                            const double df = w->fd[e + nE * m] - w->fd[e + nE * n];
+                            for (int q = 0; q < 9; ++q) koh[q + 9 * (h + (size_t)nW * e)] += I * v[q] / den * df;
+                        }
+                    }
+                }
+        }
     }
 }
 
@@ -488,7 +531,9 @@ int oracle_run(const oracle_model *md, const oracle_job *jb, int64_t k_begin, in
     nthreads = 1;
 #endif
     const size_t sz_e = (size_t)nE, sz_9e = 9 * (size_t)nE, sz_9v = 9 * (size_t)(nv > 0 ? nv : 1);
-    const size_t per = sz_e + 4 * sz_9e + 3 * sz_9v;
+    const int omega = jb->do_ahc && jb->n_hw > 0 && jb->hw_lst && out->velo_ahc && out->kubo_ohc;
+    const size_t sz_w = omega ? 9 * (size_t)jb->n_hw * nE : 0;   /* complex elements per tensor */
+    const size_t per = sz_e + 4 * sz_9e + 3 * sz_9v + 4 * sz_w;
     double *part = calloc((size_t)nthreads * per, sizeof(double));
     int64_t *cnt = calloc(nthreads, sizeof(int64_t));
     int err = 0;
@@ -502,7 +547,10 @@ int oracle_run(const oracle_model *md, const oracle_job *jb, int64_t k_begin, in
         double *p = part + (size_t)t * per;
         double *Ne = p, *ahc = Ne + sz_e, *kic = ahc + sz_9e, *klc = kic + sz_9e, *kcs = klc + sz_9e;
         double *mic = kcs + sz_9e, *mlc = mic + sz_9v, *mcs = mlc + sz_9v;
+        zc *vah = (zc *)(mcs + sz_9v), *koh = vah + sz_w;
         ws_t w = ws_alloc(N, nE);
+        oracle_job jl = *jb;
+        if (!omega) jl.n_hw = 0;
         zc *Abar = md->r ? calloc(3 * (size_t)N * N, sizeof(zc)) : 0;
 #pragma omp for schedule(static)
         for (int64_t s = 0; s < k_count; ++s) {
@@ -514,7 +562,7 @@ int oracle_run(const oracle_model *md, const oracle_job *jb, int64_t k_begin, in
                 err = rc;
                 continue;
             }
-            band_sums(md, jb, &w, Ne, ahc, mic, mlc, mcs, kic, klc, kcs);
+            band_sums(md, &jl, &w, Ne, ahc, mic, mlc, mcs, kic, klc, kcs, vah, koh);
             cnt[t] += 1;
         }
         free(Abar);
@@ -536,6 +584,13 @@ int oracle_run(const oracle_model *md, const oracle_job *jb, int64_t k_begin, in
             out->mep_ic[i] += mic[i];
             out->mep_lc[i] += mlc[i];
             out->mep_cs[i] += mcs[i];
+        }
+        const zc *vah = (const zc *)(mcs + sz_9v), *koh = vah + sz_w;
+        for (size_t i = 0; i < sz_w; ++i) {
+            out->velo_ahc[2 * i] += creal(vah[i]);
+            out->velo_ahc[2 * i + 1] += cimag(vah[i]);
+            out->kubo_ohc[2 * i] += creal(koh[i]);
+            out->kubo_ohc[2 * i + 1] += cimag(koh[i]);
         }
         out->n_k += cnt[t];
     }

@@ -38,14 +38,16 @@ class _Model(C.Structure):
 class _Job(C.Structure):
     _fields_ = [("mp_grid", C.c_int32 * 3), ("n_eF", C.c_int32), ("ef_lst", C.c_void_p),
                 ("T_kelvin", C.c_double), ("valence_bands", C.c_int32),
-                ("do_ahc", C.c_int32), ("do_mep", C.c_int32), ("do_kubo", C.c_int32)]
+                ("do_ahc", C.c_int32), ("do_mep", C.c_int32), ("do_kubo", C.c_int32),
+                ("n_hw", C.c_int32), ("hw_lst", C.c_void_p), ("eta_smr", C.c_double)]
 
 
 class _Out(C.Structure):
     _fields_ = [("Ne_sum", C.c_void_p), ("ahc", C.c_void_p),
                 ("mep_ic", C.c_void_p), ("mep_lc", C.c_void_p), ("mep_cs", C.c_void_p),
                 ("kubo_mep_ic", C.c_void_p), ("kubo_mep_lc", C.c_void_p),
-                ("kubo_mep_cs", C.c_void_p), ("n_k", C.c_int64)]
+                ("kubo_mep_cs", C.c_void_p), ("n_k", C.c_int64),
+                ("velo_ahc", C.c_void_p), ("kubo_ohc", C.c_void_p)]
 
 
 def _find_zheevd():
@@ -142,6 +144,13 @@ def run(model: dict, job: dict, k_begin: int = 0, k_count=None, k_stride: int = 
            "mep_cs": np.zeros((3, 3, nv), order="F"),
            "kubo_mep_ic": np.zeros((3, 3, nE), order="F"), "kubo_mep_lc": np.zeros((3, 3, nE), order="F"),
            "kubo_mep_cs": np.zeros((3, 3, nE), order="F")}
+    hw = job.get("hw_lst")
+    hw = None if hw is None else np.ascontiguousarray(np.asarray(hw, np.float64))
+    omega = j.do_ahc and hw is not None and hw.size > 0
+    if omega:
+        j.n_hw, j.hw_lst, j.eta_smr = hw.size, hw.ctypes.data, float(job.get("eta_smr", 0.0))
+        res["velo_ahc"] = np.zeros((3, 3, hw.size, nE), np.complex128, order="F")
+        res["kubo_ohc"] = np.zeros((3, 3, hw.size, nE), np.complex128, order="F")
     o = _Out()
     for key in res:
         setattr(o, key, res[key].ctypes.data)

@@ -19,6 +19,7 @@ of k-points, following (file:line within cMax347/MEPinterp):
 * velocity .......... src/wann_interp.f90:406-444 (get_velo)
 * occupations ....... src/statistics.f90:41-124 (fd_stat, fd_get_N_el)
 * AHC ............... src/kubo.f90:37-78 (kubo_ahc_tens)
+* optical Hall ...... src/kubo.f90:86-198 (velo_ahc_tens, kubo_ohc_tens)
 * Niu MEP ........... src/mep_niu.f90:20-159 (mep_niu_CS / _LC / _IC)
 * Kubo MEP .......... src/kubo_mep.f90:16-149 (kubo_mep_CS / _LC / _IC)
 * k-sum, Fermi pick,
@@ -339,7 +340,9 @@ def run(model: dict, job: dict, k_indices=None, batch: int = 64) -> dict:
 
     Returns the unnormalised local sums (the reference's *_loc arrays):
     Ne_sum (n_eF,), ahc (3,3,n_eF), mep_ic/lc/cs (3,3,n_val),
-    kubo_mep_ic/lc/cs (3,3,n_eF), n_k.
+    kubo_mep_ic/lc/cs (3,3,n_eF), n_k; with job["hw_lst"] (Hartree) and
+    do_ahc also velo_ahc and kubo_ohc (3,3,n_hw,n_eF) complex, smeared by
+    i * job["eta_smr"] (src/input_paras.f90:181).
     """
     mp = job["mp_grid"]
     nk_tot = int(mp[0]) * int(mp[1]) * int(mp[2])
@@ -359,6 +362,13 @@ def run(model: dict, job: dict, k_indices=None, batch: int = 64) -> dict:
     do_ahc = job.get("do_ahc", True)
     do_mep = job.get("do_mep", True)
     do_kubo = job.get("do_kubo", True)
+    hw = job.get("hw_lst")
+    do_omega = do_ahc and hw is not None and len(hw) > 0
+    if do_omega:
+        hw = np.asarray(hw, dtype=np.float64)
+        eta = float(job.get("eta_smr", 0.0))
+        out["velo_ahc"] = np.zeros((3, 3, hw.size, n_eF), complex)
+        out["kubo_ohc"] = np.zeros((3, 3, hw.size, n_eF), complex)
     for s in range(0, len(k_indices), batch):
         kidx = np.asarray(k_indices[s:s + batch])
         kpts = rel_kpts(mp, kidx)
@@ -377,6 +387,9 @@ def run(model: dict, job: dict, k_indices=None, batch: int = 64) -> dict:
             out["kubo_mep_cs"] += cs.sum(0)
         if do_ahc:
             out["ahc"] += kubo_ahc(E, V, f).sum(0)
+        if do_omega:
+            out["velo_ahc"] += velo_ahc(E, V, f, hw, eta).sum(0)
+            out["kubo_ohc"] += kubo_ohc(E, V, f, hw, eta).sum(0)
         out["n_k"] += kidx.size
     return out
 
@@ -408,7 +421,41 @@ def integrate(loc: dict, mp_grid, a_latt, n_val: int) -> dict:
         res[key] = loc[key][:, :, e] / norm
     res["kubo_mep_tens"] = res["kubo_mep_ic"] + res["kubo_mep_lc"] + res["kubo_mep_cs"]
     res["ahc_tens"] = loc["ahc"][:, :, e] / norm
+    if "velo_ahc" in loc:                                       # :501-508
+        res["ahc_velo"] = loc["velo_ahc"][:, :, :, e] / norm
+        res["ohc_velo"] = loc["kubo_ohc"][:, :, :, e] / norm
     return res
+
+
+def velo_ahc(E, V, f, hw_lst, eta):
+    """velo_ahc_tens, src/kubo.f90:86-140, per k: (nk,3,3,n_hw,n_eF) complex,
+        o(i,j,w,e) = sum_{n != n'} (f(e,n) - f(e,n')) Im(V_i(n,n') V_j(n',n))
+                                  / ((E_n - E_n')^2 - (hw_w + i eta)^2)."""
+    N = E.shape[1]
+    off = ~np.eye(N, dtype=bool)
+    dE2 = (E[:, :, None] - E[:, None, :]) ** 2                 # (k,n,n')
+    z = (np.asarray(hw_lst, dtype=np.float64) + 1j * eta) ** 2
+    with np.errstate(divide="ignore", invalid="ignore"):
+        w = np.where(off[None, :, :, None], 1.0 / (dE2[..., None] - z), 0.0)   # (k,n,n',w)
+    prod = np.einsum("kinp,kjpn->knpij", V, V).imag
+    df = f[:, :, :, None] - f[:, :, None, :]                    # (k,e,n,n')
+    return np.einsum("knpij,knpw,kenp->kijwe", prod, w, df)
+
+
+def kubo_ohc(E, V, f, hw_lst, eta):
+    """kubo_ohc_tens, src/kubo.f90:146-198, per k: (nk,3,3,n_hw,n_eF) complex,
+        z(i,j,w,e) = sum_{m != n} i V_i(n,m) V_j(m,n) (f(e,m) - f(e,n))
+                                  / ((E_m - E_n)(E_m - E_n - hw_w - i eta)),
+    with no degeneracy guard (D9)."""
+    N = E.shape[1]
+    off = ~np.eye(N, dtype=bool)
+    dE = E[:, None, :] - E[:, :, None]                         # (k,n,m) = E_m - E_n
+    hw = np.asarray(hw_lst, dtype=np.float64)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        w = np.where(off[None, :, :, None], 1.0 / (dE[..., None] * (dE[..., None] - hw - 1j * eta)), 0.0)
+    prod = np.einsum("kinm,kjmn->knmij", V, V)
+    df = f[:, :, None, :] - f[:, :, :, None]                    # (k,e,n,m) = f(e,m) - f(e,n)
+    return 1j * np.einsum("knmij,knmw,kenm->kijwe", prod, w, df)
 
 
 def velo_ahc_hw0(E, V, f, eta):

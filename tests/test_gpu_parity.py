@@ -42,6 +42,13 @@ def check_sums(gpu, ref, tol, keys=KEYS):
         assert r < tol, f"{k}: rel err {r:.3e} (max |ref| {np.abs(ref[k]).max():.3e})"
 
 
+def _check_complex(gpu, ref, tol, keys=("velo_ahc", "kubo_ohc")):
+    for k in keys:
+        scale = np.abs(ref[k]).max()
+        r = float(np.abs(np.asarray(gpu[k]) - ref[k]).max() / scale)
+        assert r < tol, f"{k}: rel err {r:.3e}"
+
+
 @pytest.fixture(scope="module")
 def model8():
     return random_tb_model(n_wf=8, r_max=1, seed=1)
@@ -89,6 +96,7 @@ def test_kloop_fp64_config1(gpu_lib):
     got = api.run(model, job, precision=api.PREC_FP64, chunk_k=1000)
     assert got["n_k"] == 4096
     check_sums(got, ref, SUM_TOL)
+    _check_complex(got, ref, SUM_TOL)
 
 
 def test_kloop_fp64_nwf32_subset(gpu_lib):
@@ -159,6 +167,7 @@ def test_mixed_config1(gpu_lib):
     got = api.run(model, job, precision=api.PREC_MIXED)
     assert got["n_k"] == 4096
     check_sums(got, ref, MIXED_TOL)
+    _check_complex(got, ref, MIXED_TOL)
 
 
 def test_mixed_fermi_sweep(gpu_lib):
@@ -239,6 +248,21 @@ def test_mixed_partial_ownership(gpu_lib):
     check_sums(got, ref, MIXED_TOL)
     got64 = api.run(m, job, precision=api.PREC_FP64, k_begin=2, k_stride=3, k_count=61)
     check_sums(got64, ref, SUM_TOL)
+
+
+@pytest.mark.parametrize("T_kelvin", [0.0, 290.1])
+def test_optical_hall_tensors(gpu_lib, T_kelvin):
+    """velo_ahc_tens and kubo_ohc_tens (src/kubo.f90:86-198) over a photon-energy
+    list and a Fermi sweep, both forms against the oracle."""
+    m = random_tb_model(n_wf=10, r_max=2, decay=1.2, seed=17)
+    job = dict(mp_grid=(5, 4, 6), ef_lst=np.linspace(-0.02, 0.02, 5), T_kelvin=T_kelvin, valence_bands=5,
+               hw_lst=np.linspace(0.0, 0.03, 4), eta_smr=0.002)
+    ref = O.run(m.as_dict(), job)
+    got = api.run(m, job, precision=api.PREC_FP64)
+    _check_complex(got, ref, SUM_TOL)
+    check_sums(got, ref, SUM_TOL)
+    mixed = api.run(m, job, precision=api.PREC_MIXED)
+    _check_complex(mixed, ref, MIXED_TOL)
 
 
 def test_run_argument_errors(gpu_lib, model8):

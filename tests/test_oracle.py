@@ -123,6 +123,26 @@ def test_numpy_vs_c(with_r, tb, gauge, sem, cart):
         assert rel(b[k], a[k]) < 1e-11, k
 
 
+def test_optical_hall_numpy_vs_c():
+    """velo_ahc_tens / kubo_ohc_tens (src/kubo.f90:86-198) in both restatements,
+    and the hw = 0, eta -> velo form against the kubo_ahc curvature sum."""
+    m = random_tb_model(n_wf=8, r_max=1, seed=13).as_dict()
+    job = dict(mp_grid=(3, 3, 4), ef_lst=np.array([-0.02, 0.0]), T_kelvin=300.0, valence_bands=4,
+               hw_lst=np.array([0.0, 0.005, 0.02]), eta_smr=0.004)
+    a = O.run(m, job)
+    b = RC.run(m, job, nthreads=2)
+    for k in ("velo_ahc", "kubo_ohc"):
+        assert a[k].shape == (3, 3, 3, 2)
+        assert np.abs(b[k] - a[k]).max() < 1e-11 * np.abs(a[k]).max(), k
+    # at hw = 0 and eta = 0 the velocity form is the Kubo AHC: the sum over
+    # ordered pairs of (f_n - f_n') Im(V V) / dE^2 regroups into the per-band
+    # curvature sum of kubo_ahc_tens
+    a0 = O.run(m, dict(job, hw_lst=np.array([0.0]), eta_smr=0.0))
+    v0 = a0["velo_ahc"][:, :, 0, :]
+    assert np.abs(v0.imag).max() == 0.0
+    assert rel(v0.real, a0["ahc"]) < 1e-10
+
+
 def test_c_interp_matches_numpy():
     m = random_tb_model(n_wf=8, r_max=1, seed=5).as_dict()
     kp = np.array([0.1, -0.2, 0.3])
