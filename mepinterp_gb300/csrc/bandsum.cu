@@ -54,6 +54,30 @@ __device__ __forceinline__ T warp_sum(T v) {
     return v;
 }
 
+// Fermi contraction of the per-band curvature, -sum_n curv(n) f(n): FP64 in
+// the FP64 form; double-FP32 in the FP32 form (curvature stored as leading
+// part + remainder), so that no FP64 instruction runs per k-point there.
+template <typename T> struct CurvSum;
+template <> struct CurvSum<double> {
+    double v;
+    __device__ __forceinline__ void zero() { v = 0.0; }
+    __device__ __forceinline__ void sub(const double* curv, const float*, const float*, int i, double f) {
+        v -= curv[i] * f;
+    }
+    __device__ __forceinline__ void warp_reduce() { v = warp_sum(v); }
+    __device__ __forceinline__ double value() const { return v; }
+};
+template <> struct CurvSum<float> {
+    DF v;
+    __device__ __forceinline__ void zero() { v = DF{0.f, 0.f}; }
+    __device__ __forceinline__ void sub(const double*, const float* cs, const float* cc, int i, float f) {
+        df_add_prod(v, -cs[i], f);
+        v.c = __fmaf_rn(-cc[i], f, v.c);
+    }
+    __device__ __forceinline__ void warp_reduce() { v = df_warp_sum(v); }
+    __device__ __forceinline__ double value() const { return (double)v.s + (double)v.c; }
+};
+
 template <typename T>
 __global__ void __launch_bounds__(256) bandsum_kernel(DevModel md, JobDev jb, int64_t nk, const double* __restrict__ Eg,
                                                       const cplx<T>* __restrict__ Vg, const T* __restrict__ CSVg,
@@ -63,7 +87,9 @@ __global__ void __launch_bounds__(256) bandsum_kernel(DevModel md, JobDev jb, in
     const int N = md.N, NN = N * N, ld = N + 1;
     const int nval = jb.nval, nE = jb.nE;
     cplx<T>* Vs = reinterpret_cast<cplx<T>*>(smem_raw);          // [3][N][ld]
-    double* curv = reinterpret_cast<double*>(Vs + 3 * N * ld);    // [9][N] AHC curvature per band (FP64)
+    double* curv = reinterpret_cast<double*>(Vs + 3 * N * ld);    // [9][N] AHC curvature per band: FP64, or
+    float* curvS = reinterpret_cast<float*>(curv);                 // in the FP32 form the leading parts [9][N]
+    float* curvC = curvS + 9 * N;                                  // and remainders [9][N] (same bytes)
     double* Es = curv + 9 * N;                                    // [kMaxN] energies (FP64)
     T* icn = reinterpret_cast<T*>(Es + kMaxN);                    // [9][N] Kubo IC per band
     T* lcn = icn + 9 * N;                                         // [9][N] Kubo LC per band
@@ -200,17 +226,19 @@ __global__ void __launch_bounds__(256) bandsum_kernel(DevModel md, JobDev jb, in
             }
 #pragma unroll
             for (int q = 0; q < 9; ++q) {
-                double a;
-                if constexpr (sizeof(T) == 4) {
-                    const DF r = df_warp_sum(s_curvf[q]);
-                    a = (double)r.s + (double)r.c;
-                } else {
-                    a = warp_sum(s_curv[q]);
-                }
+                DF rf{0.f, 0.f};
+                double a = 0.0;
+                if constexpr (sizeof(T) == 4) rf = df_warp_sum(s_curvf[q]);
+                else a = warp_sum(s_curv[q]);
                 T b = warp_sum(s_ic[q]), c = warp_sum(s_lc[q]);
                 T d = warp_sum(s_icv[q]), e = warp_sum(s_lcv[q]);
                 if (lane == 0) {
-                    curv[q * N + n0] = a;
+                    if constexpr (sizeof(T) == 4) {
+                        curvS[q * N + n0] = rf.s;
+                        curvC[q * N + n0] = rf.c;
+                    } else {
+                        curv[q * N + n0] = a;
+                    }
                     icn[q * N + n0] = b;
                     lcn[q * N + n0] = c;
                     if (n0 < kMaxN) { icv[q * kMaxN + n0] = d; lcv[q * kMaxN + n0] = e; }
@@ -232,23 +260,23 @@ __global__ void __launch_bounds__(256) bandsum_kernel(DevModel md, JobDev jb, in
             for (int e = tid; e < nE; e += nt) {
                 const double ef = jb.ef[e];
                 T ne = 0, ki[9], kl[9], kc = 0;
-                double a[9];
+                CurvSum<T> a[9];
 #pragma unroll
-                for (int q = 0; q < 9; ++q) { a[q] = 0.0; ki[q] = kl[q] = 0; }
+                for (int q = 0; q < 9; ++q) { a[q].zero(); ki[q] = kl[q] = 0; }
                 for (int n = 0; n < N; ++n) {
                     const T f = fd_stat<T>(Es[n], ef, jb.T_kelvin);
                     ne += f;
                     kc += f * Cs[n];
 #pragma unroll
                     for (int q = 0; q < 9; ++q) {
-                        a[q] -= curv[q * N + n] * (double)f;
+                        a[q].sub(curv, curvS, curvC, q * N + n, f);
                         ki[q] += icn[q * N + n] * f;
                         kl[q] += lcn[q * N + n] * f;
                     }
                 }
                 P[L.ne_off() + e] += ne;
                 if (jb.do_ahc)
-                    for (int q = 0; q < 9; ++q) P[L.ahc_off() + q + 9 * e] += a[q];
+                    for (int q = 0; q < 9; ++q) P[L.ahc_off() + q + 9 * e] += a[q].value();
                 if (jb.do_kubo) {
                     for (int q = 0; q < 9; ++q) {
                         P[L.kic_off() + q + 9 * e] += ki[q];
@@ -263,16 +291,16 @@ __global__ void __launch_bounds__(256) bandsum_kernel(DevModel md, JobDev jb, in
             for (int e = warp; e < nE; e += nwarps) {
                 const double ef = jb.ef[e];
                 T ne = 0, ki[9], kl[9], kc = 0;
-                double a[9];
+                CurvSum<T> a[9];
 #pragma unroll
-                for (int q = 0; q < 9; ++q) { a[q] = 0.0; ki[q] = kl[q] = 0; }
+                for (int q = 0; q < 9; ++q) { a[q].zero(); ki[q] = kl[q] = 0; }
                 for (int n = lane; n < N; n += 32) {
                     const T f = fd_stat<T>(Es[n], ef, jb.T_kelvin);
                     ne += f;
                     kc += f * Cs[n];
 #pragma unroll
                     for (int q = 0; q < 9; ++q) {
-                        a[q] -= curv[q * N + n] * (double)f;
+                        a[q].sub(curv, curvS, curvC, q * N + n, f);
                         ki[q] += icn[q * N + n] * f;
                         kl[q] += lcn[q * N + n] * f;
                     }
@@ -280,11 +308,11 @@ __global__ void __launch_bounds__(256) bandsum_kernel(DevModel md, JobDev jb, in
                 ne = warp_sum(ne);
                 kc = warp_sum(kc);
 #pragma unroll
-                for (int q = 0; q < 9; ++q) { a[q] = warp_sum(a[q]); ki[q] = warp_sum(ki[q]); kl[q] = warp_sum(kl[q]); }
+                for (int q = 0; q < 9; ++q) { a[q].warp_reduce(); ki[q] = warp_sum(ki[q]); kl[q] = warp_sum(kl[q]); }
                 if (lane == 0) {
                     P[L.ne_off() + e] += ne;
                     if (jb.do_ahc)
-                        for (int q = 0; q < 9; ++q) P[L.ahc_off() + q + 9 * e] += a[q];
+                        for (int q = 0; q < 9; ++q) P[L.ahc_off() + q + 9 * e] += a[q].value();
                     if (jb.do_kubo) {
                         for (int q = 0; q < 9; ++q) {
                             P[L.kic_off() + q + 9 * e] += ki[q];
@@ -310,18 +338,22 @@ __global__ void __launch_bounds__(256) bandsum_kernel(DevModel md, JobDev jb, in
 // Warp w takes the rows n = w, w + nwarps, ...; its lanes the columns m.  For
 // each (w, e) the per-row sums go to shared memory and are added over rows in
 // a fixed order into the CTA's FP64 slice, so the result is deterministic.
-// The band-energy differences entering the denominators are formed in FP64
-// (so that nothing cancels in T near a resonance E_n - E_m = +-hw); weights,
-// products and the per-row sums are in T, the sum over rows and k in FP64.
+// The band-energy differences are formed once per k in FP64 and kept as two
+// T parts, so that (E_n - E_m) -+ hw cancels without loss near a resonance;
+// weights, products and the per-row sums are in T, the sum over rows in
+// double-T (TwoSum) and the sum over k in FP64.
 template <typename T>
 __global__ void __launch_bounds__(256) opt_hall_kernel(DevModel md, JobDev jb, int64_t nk, const double* __restrict__ Eg,
                                                        const cplx<T>* __restrict__ Vg, const int* __restrict__ skip,
                                                        double* __restrict__ partials) {
     extern __shared__ unsigned char smem_raw[];
     const int N = md.N, NN = N * N, ld = N + 1;
-    cplx<T>* Vs = reinterpret_cast<cplx<T>*>(smem_raw);          // [3][N][ld]
-    double* rowacc = reinterpret_cast<double*>(Vs + 3 * N * ld);  // [N][36]
-    __shared__ double Es[kMaxN], fs[kMaxN];
+    cplx<T>* Vs = reinterpret_cast<cplx<T>*>(smem_raw);   // [3][N][ld]
+    T* dEh = reinterpret_cast<T*>(Vs + 3 * N * ld);        // [N][N] E_n - E_m (FP64 difference, leading part)
+    T* dEl = dEh + NN;                                     // [N][N] its remainder (0 in FP64)
+    T* rowacc = dEl + NN;                                  // [N][36]
+    __shared__ double Es[kMaxN];
+    __shared__ T fs[kMaxN];
     const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nwarps = nt >> 5;
     const AccLayout L{jb.nE, jb.nval, jb.nW};
     double* P = partials + (size_t)blockIdx.x * L.size();
@@ -333,12 +365,21 @@ __global__ void __launch_bounds__(256) opt_hall_kernel(DevModel md, JobDev jb, i
             Vs[(a * N + r / N) * ld + r % N] = Vg[(size_t)k * 3 * NN + e];
         }
         for (int n = tid; n < N; n += nt) Es[n] = Eg[(size_t)k * N + n];
+        __syncthreads();
+        // energy differences once per k in FP64, split into two T parts so
+        // that (E_n - E_m) -+ hw below cancels without loss near a resonance
+        for (int e = tid; e < NN; e += nt) {
+            const double d = Es[e / N] - Es[e % N];
+            const T hi = (T)d;
+            dEh[e] = hi;
+            dEl[e] = (T)(d - (double)hi);
+        }
         for (int e = 0; e < jb.nE; ++e) {
             __syncthreads();
-            for (int n = tid; n < N; n += nt) fs[n] = fd_stat<double>(Es[n], jb.ef[e], jb.T_kelvin);
+            for (int n = tid; n < N; n += nt) fs[n] = (T)fd_stat<double>(Es[n], jb.ef[e], jb.T_kelvin);
             for (int w = 0; w < jb.nW; ++w) {
                 __syncthreads();
-                const double hw = jb.hw[w];
+                const T hwh = (T)jb.hw[w], hwl = (T)(jb.hw[w] - (double)hwh);
                 const T eta = (T)jb.eta;
                 for (int n = warp; n < N; n += nwarps) {
                     T ov[18], oz[18];   // (re, im) of the 9 components
@@ -346,20 +387,17 @@ __global__ void __launch_bounds__(256) opt_hall_kernel(DevModel md, JobDev jb, i
                     for (int q = 0; q < 18; ++q) ov[q] = oz[q] = (T)0;
                     for (int m = lane; m < N; m += 32) {
                         if (m == n) continue;
-                        // the differences in FP64, so that no cancellation near a
-                        // resonance (E_n - E_m = +-hw) is left to the working precision
-                        const double dnm = Es[n] - Es[m];
-                        const T dm = (T)(dnm - hw), dp = (T)(dnm + hw), d = (T)dnm, dh = (T)(-dnm - hw);
+                        const T dh = dEh[n * N + m], dl = dEl[n * N + m];
+                        const T dm = ((dh - hwh) + dl) - hwl, dp = ((dh + hwh) + dl) + hwl, d = dh + dl;
                         // velo: (f_n - f_m) / ((E_n - E_m)^2 - (hw + i eta)^2)
                         //     = (f_n - f_m) / ((d - hw)(d + hw) + eta^2 - 2 i hw eta)
-                        const T ar = dm * dp + eta * eta, ai = -(T)2 * (T)hw * eta;
-                        const T dfv = (T)(fs[n] - fs[m]);
-                        const T vin = dfv / (ar * ar + ai * ai);
+                        const T ar = dm * dp + eta * eta, ai = -(T)2 * hwh * eta;
+                        const T vin = (fs[n] - fs[m]) / (ar * ar + ai * ai);
                         const T vr = ar * vin, vi = -ai * vin;
-                        // ohc: i (f_m - f_n) / ((E_m - E_n)(E_m - E_n - hw - i eta)),  E_m - E_n = -d
-                        const T br = -d * dh, bi = d * eta;
-                        const T dfo = (T)(fs[m] - fs[n]);
-                        const T oin = dfo / (br * br + bi * bi);
+                        // ohc: i (f_m - f_n) / ((E_m - E_n)(E_m - E_n - hw - i eta)),  E_m - E_n = -d:
+                        //     denominator d (d + hw) + i d eta
+                        const T br = d * dp, bi = d * eta;
+                        const T oin = (fs[m] - fs[n]) / (br * br + bi * bi);
                         const T orr = bi * oin, oi = br * oin;   // i (br - i bi) / |b|^2
 #pragma unroll
                         for (int j = 0; j < 3; ++j)
@@ -377,15 +415,22 @@ __global__ void __launch_bounds__(256) opt_hall_kernel(DevModel md, JobDev jb, i
                     for (int q = 0; q < 18; ++q) {
                         const T a = warp_sum(ov[q]), b = warp_sum(oz[q]);
                         if (lane == 0) {
-                            rowacc[n * 36 + q] = (double)a;
-                            rowacc[n * 36 + 18 + q] = (double)b;
+                            rowacc[n * 36 + q] = a;
+                            rowacc[n * 36 + 18 + q] = b;
                         }
                     }
                 }
                 __syncthreads();
                 for (int q = tid; q < 36; q += nt) {
-                    double acc = 0.0;
-                    for (int n = 0; n < N; ++n) acc += rowacc[n * 36 + q];
+                    double acc;
+                    if constexpr (sizeof(T) == 4) {
+                        DF r{0.f, 0.f};
+                        for (int n = 0; n < N; ++n) df_add(r, rowacc[n * 36 + q]);
+                        acc = (double)r.s + (double)r.c;
+                    } else {
+                        acc = 0.0;
+                        for (int n = 0; n < N; ++n) acc += rowacc[n * 36 + q];
+                    }
                     const int base = q < 18 ? L.vah_off() : L.koh_off();
                     P[base + (q % 18) + 18 * (w + jb.nW * e)] += acc;
                 }
@@ -437,7 +482,7 @@ template <typename T>
 cudaError_t launch_opt_hall(const DevModel& m, const JobDev& j, int64_t nk, const double* E, const cplx<T>* V,
                             const int* skip, double* partials, int n_cta, cudaStream_t s) {
     if (nk <= 0 || j.nW <= 0) return cudaSuccess;
-    const size_t smem = 3 * (size_t)m.N * (m.N + 1) * sizeof(cplx<T>) + (size_t)m.N * 36 * sizeof(double);
+    const size_t smem = 3 * (size_t)m.N * (m.N + 1) * sizeof(cplx<T>) + (2 * (size_t)m.N * m.N + (size_t)m.N * 36) * sizeof(T);
     cudaError_t e = cudaFuncSetAttribute(opt_hall_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     opt_hall_kernel<T><<<n_cta, 256, smem, s>>>(m, j, nk, E, V, skip, partials);

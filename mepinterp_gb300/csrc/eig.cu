@@ -293,7 +293,7 @@ cudaError_t launch_eig(int N, int64_t nk, const cplx<T>* W, int nbW, const cplx<
     };
     if (N <= 8) return go(jacobi_kernel<T, 8>, 8, 64);
     if (N <= 16) return go(jacobi_kernel<T, 16>, 16, 128);
-    if (N <= 32) return go(jacobi_kernel<T, 32>, 32, 256);
+    if (N <= 32) return go(jacobi_kernel<T, 32>, 32, 128);
     if (N <= 64) return go(jacobi_kernel<T, 64>, 64, 256);
     return cudaErrorInvalidValue;
 }
@@ -335,7 +335,7 @@ __global__ void __launch_bounds__(256) refine_kernel(int N, const cplx<double>* 
     cplx<float>* Us = Hl + NPP;
     cplx<float>* Rs = Us + NPP;
     cplx<float>* Ps = Rs + NPP;
-    __shared__ float ls[kMaxN];
+    __shared__ float ls[kMaxN], rh[kMaxN], rl[kMaxN];
     __shared__ int s_flag;
     const int tid = threadIdx.x, nt = blockDim.x;
     const int64_t k = blockIdx.x;
@@ -409,16 +409,23 @@ __global__ void __launch_bounds__(256) refine_kernel(int N, const cplx<double>* 
         Sn[n] = sq;
     }
     __syncthreads();
-    for (int n = tid; n < N; n += nt) rho[n] = (double)ls[n] + (double)Ps[n * Np + n].re / Sn[n];
+    for (int n = tid; n < N; n += nt) {
+        const double r = (double)ls[n] + (double)Ps[n * Np + n].re / Sn[n];
+        rho[n] = r;
+        rh[n] = (float)r;
+        rl[n] = (float)(r - (double)rh[n]);
+    }
     __syncthreads();
-    // inverse gaps 1 / (rho_n - rho_m): the degeneracy decision on the FP64
-    // difference, the reciprocal in FP32 (it scales corrections of order |P|/gap)
+    // inverse gaps 1 / (rho_n - rho_m): the difference of two FP32 hi + lo
+    // pairs (exact for close energies, where it matters), the reciprocal in
+    // FP32 (it scales corrections of order |P|/gap)
+    const float dgap = (float)degen_gap;
     for (int e = tid; e < NPP; e += nt) {
         const int m = e / Np, n = e % Np;
         float iv = 0.f;
         if (m < N && n < N && m != n) {
-            const double d = rho[n] - rho[m];
-            if (fabs(d) > degen_gap) iv = 1.f / (float)d;
+            const float d = (rh[n] - rh[m]) + (rl[n] - rl[m]);
+            if (fabsf(d) > dgap) iv = 1.f / d;
             else s_flag = 1;
         }
         Iv[e] = iv;
