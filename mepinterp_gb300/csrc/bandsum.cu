@@ -329,32 +329,39 @@ __global__ void __launch_bounds__(256) bandsum_kernel(DevModel md, JobDev jb, in
 }
 
 // Optical Hall tensors of one rank's k-points (the reference computes them
-// with do_ahc, src/core.f90:221-230), per ordered band pair n != m with
-// c_ij = V_i(n,m) V_j(m,n):
+// with do_ahc, src/core.f90:221-230):
 //   velo_ahc_tens (src/kubo.f90:86-140)
-//       o(i,j,w,e) += (f(e,n) - f(e,m)) Im(c_ij) / ((E_n - E_m)^2 - (hw_w + i eta)^2)
+//       o(i,j,w,e) = sum_{n != m} (f(e,n) - f(e,m)) Im(c_nm) Wv_nm,
+//       Wv_nm = 1 / ((E_n - E_m)^2 - (hw_w + i eta)^2)
 //   kubo_ohc_tens (src/kubo.f90:146-198), no degeneracy guard (D9)
-//       z(i,j,w,e) += i c_ij (f(e,m) - f(e,n)) / ((E_m - E_n)(E_m - E_n - hw_w - i eta))
-// Warp w takes the rows n = w, w + nwarps, ...; its lanes the columns m.  For
-// each (w, e) the per-row sums go to shared memory and are added over rows in
-// a fixed order into the CTA's FP64 slice, so the result is deterministic.
-// The band-energy differences are formed once per k in FP64 and kept as two
-// T parts, so that (E_n - E_m) -+ hw cancels without loss near a resonance;
-// weights, products and the per-row sums are in T, the sum over rows in
-// double-T (TwoSum) and the sum over k in FP64.
+//       z(i,j,w,e) = sum_{n != m} g_nm (f(e,m) - f(e,n)),
+//       g_nm = i c_nm / ((E_m - E_n)(E_m - E_n - hw_w - i eta))
+// with c_nm(i,j) = V_i(n,m) V_j(m,n).  Both are regrouped by band,
+//       o = sum_n f(e,n) Yv_n,  Yv_n = sum_m (Im c_nm - Im c_mn) Wv_nm   (Wv symmetric)
+//       z = sum_n f(e,n) Yo_n,  Yo_n = sum_m (g_mn - g_nm),
+// so a Fermi sweep costs N (n_eF + N) per photon energy instead of N^2 n_eF.
+// The pair terms of two bands of equal occupation cancel in sum_n f Y_n only
+// as far as Y_n is exact, so in the FP32 form the per-band sums and the
+// contraction run in double-FP32 (TwoSum), as for the AHC curvature.  The
+// energy differences are formed once per k in FP64 and kept as two T parts,
+// so that (E_n - E_m) -+ hw cancels without loss near a resonance.
 template <typename T>
 __global__ void __launch_bounds__(256) opt_hall_kernel(DevModel md, JobDev jb, int64_t nk, const double* __restrict__ Eg,
                                                        const cplx<T>* __restrict__ Vg, const int* __restrict__ skip,
                                                        double* __restrict__ partials) {
+    constexpr bool f32 = sizeof(T) == 4;
+    constexpr int ET = f32 ? 64 : 8;   // Fermi energies per occupation tile
     extern __shared__ unsigned char smem_raw[];
     const int N = md.N, NN = N * N, ld = N + 1;
-    cplx<T>* Vs = reinterpret_cast<cplx<T>*>(smem_raw);   // [3][N][ld]
-    T* dEh = reinterpret_cast<T*>(Vs + 3 * N * ld);        // [N][N] E_n - E_m (FP64 difference, leading part)
-    T* dEl = dEh + NN;                                     // [N][N] its remainder (0 in FP64)
-    T* rowacc = dEl + NN;                                  // [N][36]
-    __shared__ double Es[kMaxN];
-    __shared__ T fs[kMaxN];
     const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nwarps = nt >> 5;
+    cplx<T>* Vs = reinterpret_cast<cplx<T>*>(smem_raw);   // [3][N][ld]
+    T* Ys = reinterpret_cast<T*>(Vs + 3 * N * ld);         // [N][36] per-band sums (leading part)
+    T* Yc = Ys + N * 36;                                   // [N][36] remainders (FP32 form only)
+    T* fs = f32 ? Yc + N * 36 : Yc;                        // [ET][N] occupations of one tile of Fermi energies
+    T* dEh = fs + ET * N;                                  // FP32 form: [N][N] E_n - E_m, leading part
+    T* dEl = dEh + NN;                                     //            and remainder
+    T* part = dEl + NN;                                    //            [nwarps][32][36] lane terms
+    __shared__ double Es[kMaxN];
     const AccLayout L{jb.nE, jb.nval, jb.nW};
     double* P = partials + (size_t)blockIdx.x * L.size();
     for (int64_t k = blockIdx.x; k < nk; k += gridDim.x) {
@@ -365,74 +372,108 @@ __global__ void __launch_bounds__(256) opt_hall_kernel(DevModel md, JobDev jb, i
             Vs[(a * N + r / N) * ld + r % N] = Vg[(size_t)k * 3 * NN + e];
         }
         for (int n = tid; n < N; n += nt) Es[n] = Eg[(size_t)k * N + n];
-        __syncthreads();
-        // energy differences once per k in FP64, split into two T parts so
-        // that (E_n - E_m) -+ hw below cancels without loss near a resonance
-        for (int e = tid; e < NN; e += nt) {
-            const double d = Es[e / N] - Es[e % N];
-            const T hi = (T)d;
-            dEh[e] = hi;
-            dEl[e] = (T)(d - (double)hi);
-        }
-        for (int e = 0; e < jb.nE; ++e) {
+        if constexpr (f32) {
             __syncthreads();
-            for (int n = tid; n < N; n += nt) fs[n] = (T)fd_stat<double>(Es[n], jb.ef[e], jb.T_kelvin);
-            for (int w = 0; w < jb.nW; ++w) {
-                __syncthreads();
-                const T hwh = (T)jb.hw[w], hwl = (T)(jb.hw[w] - (double)hwh);
-                const T eta = (T)jb.eta;
-                for (int n = warp; n < N; n += nwarps) {
-                    T ov[18], oz[18];   // (re, im) of the 9 components
+            for (int e = tid; e < NN; e += nt) {
+                const double d = Es[e / N] - Es[e % N];
+                const T hi = (T)d;
+                dEh[e] = hi;
+                dEl[e] = (T)(d - (double)hi);
+            }
+        }
+        for (int w = 0; w < jb.nW; ++w) {
+            __syncthreads();
+            const double hwd = jb.hw[w];
+            const T hwh = (T)hwd, hwl = (T)(hwd - (double)hwh), eta = (T)jb.eta;
+            // per-band sums Y_n: warp per band, lanes over m
+            for (int n = warp; n < N; n += nwarps) {
+                T acc[36];
 #pragma unroll
-                    for (int q = 0; q < 18; ++q) ov[q] = oz[q] = (T)0;
-                    for (int m = lane; m < N; m += 32) {
-                        if (m == n) continue;
+                for (int q = 0; q < 36; ++q) acc[q] = (T)0;
+                for (int m = lane; m < N; m += 32) {
+                    if (m == n) continue;
+                    T d, dm, dp;
+                    if constexpr (f32) {
                         const T dh = dEh[n * N + m], dl = dEl[n * N + m];
-                        const T dm = ((dh - hwh) + dl) - hwl, dp = ((dh + hwh) + dl) + hwl, d = dh + dl;
-                        // velo: (f_n - f_m) / ((E_n - E_m)^2 - (hw + i eta)^2)
-                        //     = (f_n - f_m) / ((d - hw)(d + hw) + eta^2 - 2 i hw eta)
-                        const T ar = dm * dp + eta * eta, ai = -(T)2 * hwh * eta;
-                        const T vin = (fs[n] - fs[m]) / (ar * ar + ai * ai);
-                        const T vr = ar * vin, vi = -ai * vin;
-                        // ohc: i (f_m - f_n) / ((E_m - E_n)(E_m - E_n - hw - i eta)),  E_m - E_n = -d:
-                        //     denominator d (d + hw) + i d eta
-                        const T br = d * dp, bi = d * eta;
-                        const T oin = (fs[m] - fs[n]) / (br * br + bi * bi);
-                        const T orr = bi * oin, oi = br * oin;   // i (br - i bi) / |b|^2
-#pragma unroll
-                        for (int j = 0; j < 3; ++j)
-#pragma unroll
-                            for (int i = 0; i < 3; ++i) {
-                                const cplx<T> c = Vs[(i * N + n) * ld + m] * Vs[(j * N + m) * ld + n];
-                                const int q = 2 * (i + 3 * j);
-                                ov[q] += c.im * vr;
-                                ov[q + 1] += c.im * vi;
-                                oz[q] += c.re * orr - c.im * oi;
-                                oz[q + 1] += c.re * oi + c.im * orr;
-                            }
+                        d = dh + dl;
+                        dm = ((dh - hwh) + dl) - hwl;
+                        dp = ((dh + hwh) + dl) + hwl;
+                    } else {
+                        const double dd = Es[n] - Es[m];
+                        d = dd;
+                        dm = dd - hwd;
+                        dp = dd + hwd;
                     }
+                    // Wv = (ar + 2 i hw eta) / |A|^2,  A = (d - hw)(d + hw) + eta^2 - 2 i hw eta
+                    const T ar = dm * dp + eta * eta, ai = (T)2 * hwh * eta;
+                    const T an = (T)1 / (ar * ar + ai * ai);
+                    const T wvr = ar * an, wvi = ai * an;
+                    // g_nm = c_nm (B1i + i B1r) / |B1|^2,  B1 = d (d + hw) + i d eta
+                    // g_mn = c_mn (B2i + i B2r) / |B2|^2,  B2 = d (d - hw) - i d eta
+                    const T b1r = d * dp, b1i = d * eta, b2r = d * dm, b2i = -d * eta;
+                    const T n1 = (T)1 / (b1r * b1r + b1i * b1i), n2 = (T)1 / (b2r * b2r + b2i * b2i);
+                    const T g1r = b1i * n1, g1i = b1r * n1, g2r = b2i * n2, g2i = b2r * n2;
 #pragma unroll
-                    for (int q = 0; q < 18; ++q) {
-                        const T a = warp_sum(ov[q]), b = warp_sum(oz[q]);
-                        if (lane == 0) {
-                            rowacc[n * 36 + q] = a;
-                            rowacc[n * 36 + 18 + q] = b;
+                    for (int j = 0; j < 3; ++j)
+#pragma unroll
+                        for (int i = 0; i < 3; ++i) {
+                            const cplx<T> cnm = Vs[(i * N + n) * ld + m] * Vs[(j * N + m) * ld + n];
+                            const cplx<T> cmn = Vs[(i * N + m) * ld + n] * Vs[(j * N + n) * ld + m];
+                            const int q = 2 * (i + 3 * j);
+                            const T dv = cnm.im - cmn.im;
+                            acc[q] += dv * wvr;
+                            acc[q + 1] += dv * wvi;
+                            // g_mn - g_nm
+                            acc[18 + q] += (cmn.re * g2r - cmn.im * g2i) - (cnm.re * g1r - cnm.im * g1i);
+                            acc[18 + q + 1] += (cmn.re * g2i + cmn.im * g2r) - (cnm.re * g1i + cnm.im * g1r);
                         }
+                }
+                if constexpr (f32) {
+                    T* pw = part + warp * 32 * 36;
+#pragma unroll
+                    for (int q = 0; q < 36; ++q) pw[lane * 36 + q] = acc[q];
+                    __syncwarp();
+                    for (int q = lane; q < 36; q += 32) {
+                        DF r{0.f, 0.f};
+                        for (int l = 0; l < 32; ++l) df_add(r, pw[l * 36 + q]);
+                        Ys[n * 36 + q] = r.s;
+                        Yc[n * 36 + q] = r.c;
+                    }
+                    __syncwarp();
+                } else {
+#pragma unroll
+                    for (int q = 0; q < 36; ++q) {
+                        const T v = warp_sum(acc[q]);
+                        if (lane == 0) Ys[n * 36 + q] = v;
                     }
                 }
+            }
+            // contraction with the occupations, tile by tile of Fermi energies
+            for (int e0 = 0; e0 < jb.nE; e0 += ET) {
+                const int ne = min(ET, jb.nE - e0);
                 __syncthreads();
-                for (int q = tid; q < 36; q += nt) {
-                    double acc;
-                    if constexpr (sizeof(T) == 4) {
+                for (int t = tid; t < ne * N; t += nt) {
+                    const int e = t / N, n = t % N;
+                    fs[e * N + n] = (T)fd_stat<double>(Es[n], jb.ef[e0 + e], jb.T_kelvin);
+                }
+                __syncthreads();
+                for (int t = tid; t < ne * 36; t += nt) {
+                    const int e = t / 36, q = t % 36;
+                    double v;
+                    if constexpr (f32) {
                         DF r{0.f, 0.f};
-                        for (int n = 0; n < N; ++n) df_add(r, rowacc[n * 36 + q]);
-                        acc = (double)r.s + (double)r.c;
+                        for (int n = 0; n < N; ++n) {
+                            const float f = fs[e * N + n];
+                            df_add_prod(r, Ys[n * 36 + q], f);
+                            r.c = __fmaf_rn(Yc[n * 36 + q], f, r.c);
+                        }
+                        v = (double)r.s + (double)r.c;
                     } else {
-                        acc = 0.0;
-                        for (int n = 0; n < N; ++n) acc += rowacc[n * 36 + q];
+                        v = 0.0;
+                        for (int n = 0; n < N; ++n) v += Ys[n * 36 + q] * fs[e * N + n];
                     }
                     const int base = q < 18 ? L.vah_off() : L.koh_off();
-                    P[base + (q % 18) + 18 * (w + jb.nW * e)] += acc;
+                    P[base + (q % 18) + 18 * (w + jb.nW * (e0 + e))] += v;
                 }
             }
         }
@@ -482,8 +523,13 @@ template <typename T>
 cudaError_t launch_opt_hall(const DevModel& m, const JobDev& j, int64_t nk, const double* E, const cplx<T>* V,
                             const int* skip, double* partials, int n_cta, cudaStream_t s) {
     if (nk <= 0 || j.nW <= 0) return cudaSuccess;
-    const size_t smem = 3 * (size_t)m.N * (m.N + 1) * sizeof(cplx<T>) + (2 * (size_t)m.N * m.N + (size_t)m.N * 36) * sizeof(T);
+    const size_t N = m.N, ET = sizeof(T) == 4 ? 64 : 8;
+    size_t smem = 3 * N * (N + 1) * sizeof(cplx<T>) + (N * 36 + ET * N) * sizeof(T);
+    if (sizeof(T) == 4) smem += (N * 36 + 2 * N * N + 8 * 32 * 36) * sizeof(T);   // Yc, dEh, dEl, part
     cudaError_t e = cudaFuncSetAttribute(opt_hall_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(opt_hall_kernel<T>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 cudaSharedmemCarveoutMaxShared);
     if (e != cudaSuccess) return e;
     opt_hall_kernel<T><<<n_cta, 256, smem, s>>>(m, j, nk, E, V, skip, partials);
     return cudaGetLastError();

@@ -250,12 +250,13 @@ def test_mixed_partial_ownership(gpu_lib):
     check_sums(got64, ref, SUM_TOL)
 
 
-@pytest.mark.parametrize("T_kelvin", [0.0, 290.1])
-def test_optical_hall_tensors(gpu_lib, T_kelvin):
+@pytest.mark.parametrize("T_kelvin,n_ef", [(0.0, 5), (290.1, 70)])
+def test_optical_hall_tensors(gpu_lib, T_kelvin, n_ef):
     """velo_ahc_tens and kubo_ohc_tens (src/kubo.f90:86-198) over a photon-energy
-    list and a Fermi sweep, both forms against the oracle."""
+    list and a Fermi sweep (70 energies span several occupation tiles), both
+    forms against the oracle."""
     m = random_tb_model(n_wf=10, r_max=2, decay=1.2, seed=17)
-    job = dict(mp_grid=(5, 4, 6), ef_lst=np.linspace(-0.02, 0.02, 5), T_kelvin=T_kelvin, valence_bands=5,
+    job = dict(mp_grid=(5, 4, 6), ef_lst=np.linspace(-0.02, 0.02, n_ef), T_kelvin=T_kelvin, valence_bands=5,
                hw_lst=np.linspace(0.0, 0.03, 4), eta_smr=0.002)
     ref = O.run(m.as_dict(), job)
     got = api.run(m, job, precision=api.PREC_FP64)
