@@ -150,6 +150,15 @@ typedef struct {
                                   (0 when a run reuses the slabs of its mesh) */
 } mepi_timing;
 
+/* Launch shapes of the per-k kernels of one context.  No counterpart in the
+ * reference.  0 selects the built-in choice. */
+typedef struct {
+    int32_t jacobi_threads;    /* threads per eigensolver CTA: 64, 128 or 256 */
+    int32_t jacobi_kblock;     /* k-points per eigensolver CTA, warm-started in turn */
+    int64_t chunk_k;           /* k-points per device chunk (a job's chunk_k > 0 wins) */
+    double k_per_s;            /* mepi_autotune: the measured rate of this choice */
+} mepi_tuning;
+
 /* Replaces read_tb_basis's arrays being handed to get_wann_interp
  * (src/core.f90:144, :179-182): validates and uploads the model. */
 int mepi_create(mepi_ctx **out, const mepi_model *m);
@@ -167,6 +176,26 @@ int mepi_interp_k(mepi_ctx *ctx, int32_t precision, int64_t n_k, const double *k
 
 /* Device time per stage of the last mepi_run. */
 int mepi_get_timing(const mepi_ctx *ctx, mepi_timing *t);
+
+/* Autotuner.  No counterpart in the reference.  Times the candidate launch
+ * shapes (eigensolver threads 64/128/256, warm-start run 4/8/16, chunk 16K/64K
+ * k-points) on the first sample_k k-points of the job (<= 0: 32768), keeps the
+ * fastest in the context and records it for the contexts created later in
+ * this process with the same device, band count, R count and stack blocks. */
+int mepi_autotune(mepi_ctx *ctx, const mepi_job *job, int64_t sample_k, mepi_tuning *best);
+int mepi_set_tuning(mepi_ctx *ctx, const mepi_tuning *t);
+int mepi_get_tuning(const mepi_ctx *ctx, mepi_tuning *t);
+
+/* Batched form.  No counterpart in the reference, where each model is a
+ * separate run.  n (context, job) pairs -- models of different band and R
+ * counts, each with its own mesh, Fermi sweep and precision -- run as ONE
+ * CUDA graph: every context's chunk pipeline is captured on its own stream
+ * (independent models overlap on the GPU) and the graph is launched once.
+ * The FP64 reruns of the mixed form, the reductions and the copies back
+ * follow per context.  All contexts must be on the same device.  graph_ms
+ * (optional) receives the device time of the graph launch.  Results equal
+ * those of n separate mepi_run calls. */
+int mepi_run_batch(int32_t n, mepi_ctx *const *ctxs, const mepi_job *jobs, mepi_acc *accs, double *graph_ms);
 
 /* Band sums without any device allocation.  No counterpart in the reference.
  *

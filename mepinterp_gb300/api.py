@@ -96,6 +96,15 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
     lib.mepi_get_timing.restype = C.c_int
     lib.mepi_destroy.argtypes = [P]
     lib.mepi_destroy.restype = C.c_int
+    lib.mepi_autotune.argtypes = [P, C.POINTER(MepiJob), C.c_int64, C.POINTER(MepiTuning)]
+    lib.mepi_autotune.restype = C.c_int
+    lib.mepi_set_tuning.argtypes = [P, C.POINTER(MepiTuning)]
+    lib.mepi_set_tuning.restype = C.c_int
+    lib.mepi_get_tuning.argtypes = [P, C.POINTER(MepiTuning)]
+    lib.mepi_get_tuning.restype = C.c_int
+    lib.mepi_run_batch.argtypes = [C.c_int32, C.POINTER(P), C.POINTER(MepiJob), C.POINTER(MepiAcc),
+                                   C.POINTER(C.c_double)]
+    lib.mepi_run_batch.restype = C.c_int
     lib.mepi_strerror.argtypes = [C.c_int]
     lib.mepi_strerror.restype = C.c_char_p
     lib.mepi_version.restype = C.c_char_p
@@ -188,48 +197,27 @@ class Context:
         Returns the unnormalised local sums with the reference's shapes
         (Fortran order).
         """
-        ef = np.ascontiguousarray(np.atleast_1d(np.asarray(job["ef_lst"], np.float64)))
-        nE = ef.size
-        nv = int(job["valence_bands"])
-        j = MepiJob()
-        for i in range(3):
-            j.mp_grid[i] = int(job["mp_grid"][i])
-        j.k_begin, j.k_stride, j.k_count = int(k_begin), int(k_stride), int(k_count)
-        j.n_eF, j.ef_lst = nE, ef.ctypes.data
-        j.T_kelvin = float(job.get("T_kelvin", 0.0))
-        j.valence_bands = nv
-        outs = 0
-        if job.get("do_ahc", True):
-            outs |= OUT_AHC
-        if job.get("do_mep", True):
-            outs |= OUT_MEP_NIU
-        if job.get("do_kubo", True):
-            outs |= OUT_KUBO_MEP
-        hw = job.get("hw_lst")
-        hw = None if hw is None else np.ascontiguousarray(np.atleast_1d(np.asarray(hw, np.float64)))
-        if (outs & OUT_AHC) and hw is not None and hw.size:
-            outs |= OUT_OPT_HALL
-            j.n_hw, j.hw_lst, j.eta_smr = hw.size, hw.ctypes.data, float(job.get("eta_smr", 0.0))
-        j.outputs = outs
-        j.precision = int(precision)
-        j.chunk_k = int(chunk_k)
-        j.degen_gap = float(degen_gap)
-        res = {"Ne_sum": np.zeros(nE), "ahc": np.zeros((3, 3, nE), order="F"),
-               "mep_ic": np.zeros((3, 3, nv), order="F"), "mep_lc": np.zeros((3, 3, nv), order="F"),
-               "mep_cs": np.zeros((3, 3, nv), order="F"),
-               "kubo_mep_ic": np.zeros((3, 3, nE), order="F"), "kubo_mep_lc": np.zeros((3, 3, nE), order="F"),
-               "kubo_mep_cs": np.zeros((3, 3, nE), order="F")}
-        if outs & OUT_OPT_HALL:
-            res["velo_ahc"] = np.zeros((3, 3, hw.size, nE), np.complex128, order="F")
-            res["kubo_ohc"] = np.zeros((3, 3, hw.size, nE), np.complex128, order="F")
-        acc = MepiAcc()
-        for key, arr in res.items():
-            setattr(acc, key, arr.ctypes.data if arr.size else None)
-        _check(self.lib.mepi_run(self._h, C.byref(j), C.byref(acc)))
-        res["n_k"] = int(acc.n_k_done)
-        res["n_k_fp64"] = int(acc.n_k_fp64)
-        res["eig_max_sweeps"] = int(acc.eig_max_sweeps)
-        return res
+        call = _JobCall(job, precision, k_begin, k_stride, k_count, chunk_k, degen_gap)
+        _check(self.lib.mepi_run(self._h, C.byref(call.j), C.byref(call.acc)))
+        return call.result()
+
+    def autotune(self, job: dict, precision: int = PREC_MIXED, sample_k: int = 0) -> dict:
+        """mepi_autotune: time the candidate launch shapes on the first sample_k
+        k-points of the job and keep the fastest for this context (and for
+        later contexts of the same kind in this process)."""
+        call = _JobCall(job, precision)
+        t = MepiTuning()
+        _check(self.lib.mepi_autotune(self._h, C.byref(call.j), int(sample_k), C.byref(t)))
+        return {f: getattr(t, f) for f, _ in MepiTuning._fields_}
+
+    def get_tuning(self) -> dict:
+        t = MepiTuning()
+        _check(self.lib.mepi_get_tuning(self._h, C.byref(t)))
+        return {f: getattr(t, f) for f, _ in MepiTuning._fields_}
+
+    def set_tuning(self, jacobi_threads: int = 0, jacobi_kblock: int = 0, chunk_k: int = 0) -> None:
+        t = MepiTuning(int(jacobi_threads), int(jacobi_kblock), int(chunk_k), 0.0)
+        _check(self.lib.mepi_set_tuning(self._h, C.byref(t)))
 
     def get_wann_interp(self, kpts, precision: int = PREC_FP64):
         """en_k (nk,N), V (nk,3,N,N), A_diag (nk,3,N), Om_diag (nk,3,3,N) in C order."""
@@ -251,6 +239,83 @@ class Context:
         t = MepiTiming()
         _check(self.lib.mepi_get_timing(self._h, C.byref(t)))
         return {f: getattr(t, f) for f, _ in MepiTiming._fields_}
+
+
+class MepiTuning(C.Structure):
+    _fields_ = [("jacobi_threads", C.c_int32), ("jacobi_kblock", C.c_int32), ("chunk_k", C.c_int64),
+                ("k_per_s", C.c_double)]
+
+
+class _JobCall:
+    """A mepi_job and its mepi_acc with the result arrays they point to."""
+
+    def __init__(self, job: dict, precision: int = PREC_FP64, k_begin: int = 0, k_stride: int = 1,
+                 k_count: int = -1, chunk_k: int = 0, degen_gap: float = -1.0):
+        self.ef = np.ascontiguousarray(np.atleast_1d(np.asarray(job["ef_lst"], np.float64)))
+        nE = self.ef.size
+        nv = int(job["valence_bands"])
+        j = MepiJob()
+        for i in range(3):
+            j.mp_grid[i] = int(job["mp_grid"][i])
+        j.k_begin, j.k_stride, j.k_count = int(k_begin), int(k_stride), int(k_count)
+        j.n_eF, j.ef_lst = nE, self.ef.ctypes.data
+        j.T_kelvin = float(job.get("T_kelvin", 0.0))
+        j.valence_bands = nv
+        outs = 0
+        if job.get("do_ahc", True):
+            outs |= OUT_AHC
+        if job.get("do_mep", True):
+            outs |= OUT_MEP_NIU
+        if job.get("do_kubo", True):
+            outs |= OUT_KUBO_MEP
+        hw = job.get("hw_lst")
+        self.hw = None if hw is None else np.ascontiguousarray(np.atleast_1d(np.asarray(hw, np.float64)))
+        if (outs & OUT_AHC) and self.hw is not None and self.hw.size:
+            outs |= OUT_OPT_HALL
+            j.n_hw, j.hw_lst, j.eta_smr = self.hw.size, self.hw.ctypes.data, float(job.get("eta_smr", 0.0))
+        j.outputs = outs
+        j.precision = int(precision)
+        j.chunk_k = int(chunk_k)
+        j.degen_gap = float(degen_gap)
+        self.j = j
+        self.res = {"Ne_sum": np.zeros(nE), "ahc": np.zeros((3, 3, nE), order="F"),
+                    "mep_ic": np.zeros((3, 3, nv), order="F"), "mep_lc": np.zeros((3, 3, nv), order="F"),
+                    "mep_cs": np.zeros((3, 3, nv), order="F"),
+                    "kubo_mep_ic": np.zeros((3, 3, nE), order="F"), "kubo_mep_lc": np.zeros((3, 3, nE), order="F"),
+                    "kubo_mep_cs": np.zeros((3, 3, nE), order="F")}
+        if outs & OUT_OPT_HALL:
+            self.res["velo_ahc"] = np.zeros((3, 3, self.hw.size, nE), np.complex128, order="F")
+            self.res["kubo_ohc"] = np.zeros((3, 3, self.hw.size, nE), np.complex128, order="F")
+        self.acc = MepiAcc()
+        for key, arr in self.res.items():
+            setattr(self.acc, key, arr.ctypes.data if arr.size else None)
+
+    def result(self) -> dict:
+        res = dict(self.res)
+        res["n_k"] = int(self.acc.n_k_done)
+        res["n_k_fp64"] = int(self.acc.n_k_fp64)
+        res["eig_max_sweeps"] = int(self.acc.eig_max_sweeps)
+        return res
+
+
+def run_batch(contexts, jobs, precision=PREC_MIXED):
+    """mepi_run_batch: one (context, job) pair per model, all in one CUDA graph
+    launch.  ``precision`` is one value or one per job.  Returns (list of the
+    unnormalised local sums, device time of the graph in ms)."""
+    precs = precision if isinstance(precision, (list, tuple)) else [precision] * len(jobs)
+    calls = [_JobCall(j, p) for j, p in zip(jobs, precs)]
+    n = len(calls)
+    lib = contexts[0].lib
+    ctxs = (C.c_void_p * n)(*[c._h.value for c in contexts])
+    job_arr = (MepiJob * n)(*[c.j for c in calls])
+    acc_arr = (MepiAcc * n)(*[c.acc for c in calls])
+    ms = C.c_double(0.0)
+    _check(lib.mepi_run_batch(n, ctxs, job_arr, acc_arr, C.byref(ms)))
+    out = []
+    for i, c in enumerate(calls):
+        c.acc = acc_arr[i]
+        out.append(c.result())
+    return out, float(ms.value)
 
 
 def run(model: TBModel, job: dict, precision: int = PREC_FP64, **kw) -> dict:

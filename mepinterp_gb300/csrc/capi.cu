@@ -13,6 +13,9 @@
 //              smallest band gap is below degen_gap is skipped there and rerun
 //              through the FP64 pipeline afterwards.
 #include <algorithm>
+#include <array>
+#include <mutex>
+#include <map>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -84,6 +87,20 @@ struct mepi_ctx {
     DevBuf kcol;
     std::vector<int64_t> kcol_host;
     int64_t kcol_key[6] = {-1, -1, -1, -1, -1, -1};
+    // launch shapes picked by mepi_autotune (0 = the built-in choice)
+    mepi_tuning tune{};
+    // state of the current run between its phases (prepare, enqueue, finish)
+    struct Run {
+        mepi_job job{};
+        int64_t count = 0, chunk = 0;
+        bool fp64 = true;
+        double degen_gap = 3e-3;
+        int n_hw = 0, n_cta = 0;
+        AccLayout L{1, 0, 0};
+        JobDev jb{};
+        size_t run_ev = 0;
+    } run;
+    bool timed = true;                  // per-stage CUDA events (off inside a graph capture)
 };
 
 namespace {
@@ -101,7 +118,12 @@ namespace {
         if (_e != cudaSuccess) return MEPI_ERR_CUDA;                                 \
     } while (0)
 
+constexpr size_t kNoEvent = ~(size_t)0;
 int stage_begin(mepi_ctx* c, int stage, size_t* idx) {
+    if (!c->timed) {
+        *idx = kNoEvent;
+        return 0;
+    }
     if (c->ev_used == c->events.size()) {
         StageEv ev{};
         CK(cudaEventCreate(&ev.a));
@@ -114,6 +136,7 @@ int stage_begin(mepi_ctx* c, int stage, size_t* idx) {
     return 0;
 }
 int stage_end(mepi_ctx* c, size_t idx) {
+    if (idx == kNoEvent) return 0;
     CK(cudaEventRecord(c->events[idx].b, c->stream));
     return 0;
 }
@@ -193,12 +216,14 @@ int run_chunk(mepi_ctx* ctx, const KRange& kr, const JobDev* jb, int n_cta, doub
         else
             STAGE(ST_FTH, launch_ft_h64(ctx->dm, kr, H64, ctx->stream));
         STAGE(ST_EIG, (launch_eig<T>(ctx->N, nk, ctx->W.as<cplx<T>>(), ctx->nb, H64, ctx->E.as<T>(),
-                                     ctx->U.as<cplx<T>>(), 40, counters, counters + 2, degen_gap, flags, ctx->stream)));
+                                     ctx->U.as<cplx<T>>(), 40, counters, counters + 2, degen_gap, flags, ctx->stream,
+                                     ctx->tune.jacobi_threads, ctx->tune.jacobi_kblock)));
         STAGE(ST_REFINE, launch_refine(ctx->N, nk, H64, reinterpret_cast<const float*>(ctx->E.p),
                                        reinterpret_cast<cplx<float>*>(ctx->U.p), E64, degen_gap, flags, ctx->stream));
     } else {
         STAGE(ST_EIG, (launch_eig<T>(ctx->N, nk, ctx->W.as<cplx<T>>(), ctx->nb, nullptr, reinterpret_cast<T*>(E64),
-                                     ctx->U.as<cplx<T>>(), 40, counters, counters + 1, degen_gap, flags, ctx->stream)));
+                                     ctx->U.as<cplx<T>>(), 40, counters, counters + 1, degen_gap, flags, ctx->stream,
+                                     ctx->tune.jacobi_threads, ctx->tune.jacobi_kblock)));
     }
     STAGE(ST_ROT, (launch_rot<T>(ctx->dm, nk, ctx->W.as<cplx<T>>(), ctx->U.as<cplx<T>>(), ctx->HA.as<cplx<T>>(),
                                  ctx->OD.as<cplx<T>>(), ctx->stream)));
@@ -295,7 +320,10 @@ int prepare_sep(mepi_ctx* ctx, const mepi_job* job, int64_t count, bool fp64) {
     return 0;
 }
 
-int run_impl(mepi_ctx* ctx, const mepi_job* job, mepi_acc* out) {
+// Phase 1 of a run: validate, size and allocate, build the separable slabs and
+// the k list, upload the Fermi and photon energies.  Enqueues only small
+// copies and memsets on the context's stream.
+int run_prepare(mepi_ctx* ctx, const mepi_job* job) {
     const int N = ctx->N;
     const int64_t nk_tot = (int64_t)job->mp_grid[0] * job->mp_grid[1] * job->mp_grid[2];
     if (job->mp_grid[0] <= 0 || job->mp_grid[1] <= 0 || job->mp_grid[2] <= 0) return MEPI_ERR_ARG;
@@ -303,37 +331,40 @@ int run_impl(mepi_ctx* ctx, const mepi_job* job, mepi_acc* out) {
     if (job->n_eF <= 0 || !job->ef_lst || job->valence_bands < 0 || job->valence_bands > N) return MEPI_ERR_ARG;
     if (job->precision != MEPI_PREC_FP64 && job->precision != MEPI_PREC_MIXED) return MEPI_ERR_ARG;
     if (!finite_all(job->ef_lst, job->n_eF) || !std::isfinite(job->T_kelvin)) return MEPI_ERR_ARG;
-    int64_t owned = job->k_begin < nk_tot ? (nk_tot - job->k_begin + job->k_stride - 1) / job->k_stride : 0;
-    int64_t count = job->k_count < 0 ? owned : std::min<int64_t>(job->k_count, owned);
-    const bool fp64 = job->precision == MEPI_PREC_FP64;
-    int64_t chunk = job->chunk_k > 0 ? job->chunk_k : default_chunk(N, ctx->nb, fp64);
-    chunk = std::max<int64_t>(1, std::min<int64_t>(chunk, std::max<int64_t>(count, 1)));
-    const double degen_gap = job->degen_gap >= 0 ? job->degen_gap : 3e-3;
-
     const bool opt_hall = (job->outputs & MEPI_OUT_OPT_HALL) != 0;
     if (opt_hall && (job->n_hw <= 0 || !job->hw_lst || !finite_all(job->hw_lst, job->n_hw) ||
                      !std::isfinite(job->eta_smr)))
         return MEPI_ERR_ARG;
-    const int n_hw = opt_hall ? job->n_hw : 0;
-    AccLayout L{job->n_eF, job->valence_bands, n_hw};
-    const int n_cta = bandsum_ctas();
-    CKM(ctx->partials.ensure((size_t)n_cta * L.size() * sizeof(double)));
-    CKM(ctx->out.ensure((size_t)L.size() * sizeof(double) + (size_t)(job->n_eF + n_hw) * sizeof(double)));
+    mepi_ctx::Run& r = ctx->run;
+    r.job = *job;
+    const int64_t owned = job->k_begin < nk_tot ? (nk_tot - job->k_begin + job->k_stride - 1) / job->k_stride : 0;
+    r.count = job->k_count < 0 ? owned : std::min<int64_t>(job->k_count, owned);
+    r.fp64 = job->precision == MEPI_PREC_FP64;
+    int64_t chunk = job->chunk_k > 0 ? job->chunk_k
+                  : ctx->tune.chunk_k > 0 ? ctx->tune.chunk_k : default_chunk(N, ctx->nb, r.fp64);
+    r.chunk = std::max<int64_t>(1, std::min<int64_t>(chunk, std::max<int64_t>(r.count, 1)));
+    r.degen_gap = job->degen_gap >= 0 ? job->degen_gap : 3e-3;
+    r.n_hw = opt_hall ? job->n_hw : 0;
+    r.L = AccLayout{job->n_eF, job->valence_bands, r.n_hw};
+    r.n_cta = bandsum_ctas();
+    const AccLayout& L = r.L;
+    CKM(ctx->partials.ensure((size_t)r.n_cta * L.size() * sizeof(double)));
+    CKM(ctx->out.ensure((size_t)L.size() * sizeof(double) + (size_t)(job->n_eF + r.n_hw) * sizeof(double)));
     CKM(ctx->counters.ensure(4 * sizeof(int)));
-    CK(cudaMemsetAsync(ctx->partials.p, 0, (size_t)n_cta * L.size() * sizeof(double), ctx->stream));
+    CK(cudaMemsetAsync(ctx->partials.p, 0, (size_t)r.n_cta * L.size() * sizeof(double), ctx->stream));
     CK(cudaMemsetAsync(ctx->counters.p, 0, 4 * sizeof(int), ctx->stream));
     ctx->ev_used = 0;
-    size_t run_ev;
-    if (int r0 = stage_begin(ctx, ST_RUN, &run_ev)) return r0;
+    if (int r0 = stage_begin(ctx, ST_RUN, &r.run_ev)) return r0;
     double* d_ef = ctx->out.as<double>() + L.size();
     CK(cudaMemcpyAsync(d_ef, job->ef_lst, job->n_eF * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
     ctx->h2d += job->n_eF * sizeof(double);
     double* d_hw = d_ef + job->n_eF;
-    if (n_hw) {
-        CK(cudaMemcpyAsync(d_hw, job->hw_lst, n_hw * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
-        ctx->h2d += n_hw * sizeof(double);
+    if (r.n_hw) {
+        CK(cudaMemcpyAsync(d_hw, job->hw_lst, r.n_hw * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+        ctx->h2d += r.n_hw * sizeof(double);
     }
-    JobDev jb;
+    JobDev& jb = r.jb;
+    jb = JobDev{};
     jb.nE = job->n_eF;
     jb.nval = job->valence_bands;
     jb.do_ahc = (job->outputs & MEPI_OUT_AHC) ? 1 : 0;
@@ -341,55 +372,82 @@ int run_impl(mepi_ctx* ctx, const mepi_job* job, mepi_acc* out) {
     jb.do_kubo = (job->outputs & MEPI_OUT_KUBO_MEP) ? 1 : 0;
     jb.T_kelvin = job->T_kelvin;
     jb.ef = d_ef;
-    jb.nW = n_hw;
-    jb.hw = n_hw ? d_hw : nullptr;
+    jb.nW = r.n_hw;
+    jb.hw = r.n_hw ? d_hw : nullptr;
     jb.eta = job->eta_smr;
-
-    std::vector<int64_t> redo;
-    int rc = 0;
-    rc = prepare_sep(ctx, job, count, fp64);
+    int rc = prepare_sep(ctx, job, r.count, r.fp64);
     if (rc) return rc;
-    // chunk c0..c0+cn of the run's k-points: the column-ordered list, or the
-    // rank's stride
-    auto chunk_range = [&](int64_t c0, int64_t cn) {
-        if (ctx->sep_active)
-            return KRange{0, 1, cn, ctx->kcol.as<int64_t>() + c0, nullptr,
-                          {job->mp_grid[0], job->mp_grid[1], job->mp_grid[2]}};
-        return KRange{job->k_begin + c0 * job->k_stride, job->k_stride, cn, nullptr, nullptr,
-                      {job->mp_grid[0], job->mp_grid[1], job->mp_grid[2]}};
-    };
-    if (fp64) {
-        rc = ensure_chunk<double>(ctx, chunk);
-        if (rc) return rc;
-        for (int64_t c0 = 0; c0 < count; c0 += chunk) {
-            KRange kr = chunk_range(c0, std::min(chunk, count - c0));
-            rc = run_chunk<double>(ctx, kr, &jb, n_cta, 0.0, false, true, nullptr);
-            if (rc) return rc;
-        }
-    } else {
-        rc = ensure_chunk<float>(ctx, chunk);
-        if (rc) return rc;
-        const int64_t nchunks = (count + chunk - 1) / chunk;
-        if ((size_t)count > ctx->h_flags_cap) {
+    rc = r.fp64 ? ensure_chunk<double>(ctx, r.chunk) : ensure_chunk<float>(ctx, r.chunk);
+    if (rc) return rc;
+    if (!r.fp64) {
+        if ((size_t)r.count > ctx->h_flags_cap) {
             if (ctx->h_flags) cudaFreeHost(ctx->h_flags);
             ctx->h_flags = nullptr;
             ctx->h_flags_cap = 0;
-            CKM(cudaMallocHost(&ctx->h_flags, std::max<int64_t>(count, 1) * sizeof(int)));
-            ctx->h_flags_cap = count;
+            CKM(cudaMallocHost(&ctx->h_flags, std::max<int64_t>(r.count, 1) * sizeof(int)));
+            ctx->h_flags_cap = r.count;
         }
-        for (int64_t ci = 0; ci < nchunks; ++ci) {
-            int64_t c0 = ci * chunk, cn = std::min(chunk, count - c0);
-            KRange kr = chunk_range(c0, cn);
-            rc = run_chunk<float>(ctx, kr, &jb, n_cta, degen_gap, true, true, nullptr);
+        if (!ctx->sep_active && ctx->ft_pref != 2) {
+            // the tensor-core operands, allocated here so that the enqueue phase allocates nothing
+            if (!ctx->tc.ready()) {
+                rc = tc_plan_init(ctx->tc, ctx->dm, ctx->S_host.data());
+                if (rc) return rc;
+                ctx->h2d += 2 * (int64_t)ctx->tc.ncolp * ctx->tc.Kp * sizeof(__half);
+            }
+            rc = tc_plan_rows(ctx->tc, r.chunk);
             if (rc) return rc;
-            CK(cudaMemcpyAsync(ctx->h_flags + c0, ctx->flags.p, cn * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-            ctx->d2h += cn * sizeof(int);
         }
+    }
+    return 0;
+}
+
+// chunk c0..c0+cn of the run's k-points: the column-ordered list, or the rank's stride
+KRange chunk_range(const mepi_ctx* ctx, int64_t c0, int64_t cn) {
+    const mepi_job& job = ctx->run.job;
+    if (ctx->sep_active)
+        return KRange{0, 1, cn, const_cast<mepi_ctx*>(ctx)->kcol.as<int64_t>() + c0, nullptr,
+                      {job.mp_grid[0], job.mp_grid[1], job.mp_grid[2]}};
+    return KRange{job.k_begin + c0 * job.k_stride, job.k_stride, cn, nullptr, nullptr,
+                  {job.mp_grid[0], job.mp_grid[1], job.mp_grid[2]}};
+}
+
+// Phase 2: every chunk of the run, as stream work only (no allocation, no
+// synchronisation), so that it can be captured into a CUDA graph.
+int run_enqueue(mepi_ctx* ctx) {
+    mepi_ctx::Run& r = ctx->run;
+    int rc = 0;
+    for (int64_t c0 = 0; c0 < r.count; c0 += r.chunk) {
+        const int64_t cn = std::min(r.chunk, r.count - c0);
+        const KRange kr = chunk_range(ctx, c0, cn);
+        if (r.fp64) {
+            rc = run_chunk<double>(ctx, kr, &r.jb, r.n_cta, 0.0, false, true, nullptr);
+        } else {
+            rc = run_chunk<float>(ctx, kr, &r.jb, r.n_cta, r.degen_gap, true, true, nullptr);
+            if (!rc) {
+                CK(cudaMemcpyAsync(ctx->h_flags + c0, ctx->flags.p, cn * sizeof(int), cudaMemcpyDeviceToHost,
+                                   ctx->stream));
+                ctx->d2h += cn * sizeof(int);
+            }
+        }
+        if (rc) return rc;
+    }
+    return 0;
+}
+
+// Phase 3: the FP64 reruns of the mixed form, the fixed-order reduction and
+// the copy back.
+int run_finish(mepi_ctx* ctx, mepi_acc* out) {
+    mepi_ctx::Run& r = ctx->run;
+    const mepi_job& job = r.job;
+    const AccLayout& L = r.L;
+    std::vector<int64_t> redo;
+    int rc = 0;
+    if (!r.fp64) {
         CK(cudaStreamSynchronize(ctx->stream));
-        for (int64_t i = 0; i < count; ++i)
-            if (ctx->h_flags[i]) redo.push_back(ctx->sep_active ? ctx->kcol_host[i] : job->k_begin + i * job->k_stride);
+        for (int64_t i = 0; i < r.count; ++i)
+            if (ctx->h_flags[i]) redo.push_back(ctx->sep_active ? ctx->kcol_host[i] : job.k_begin + i * job.k_stride);
         if (!redo.empty()) {
-            int64_t rchunk = std::min<int64_t>(default_chunk(N, ctx->nb, true), (int64_t)redo.size());
+            int64_t rchunk = std::min<int64_t>(default_chunk(ctx->N, ctx->nb, true), (int64_t)redo.size());
             rc = ensure_chunk<double>(ctx, rchunk);
             if (rc) return rc;
             CKM(ctx->klist.ensure(redo.size() * sizeof(int64_t)));
@@ -398,19 +456,19 @@ int run_impl(mepi_ctx* ctx, const mepi_job* job, mepi_acc* out) {
             ctx->h2d += redo.size() * sizeof(int64_t);
             for (int64_t c0 = 0; c0 < (int64_t)redo.size(); c0 += rchunk) {
                 KRange kr{0, 1, std::min<int64_t>(rchunk, (int64_t)redo.size() - c0), ctx->klist.as<int64_t>() + c0,
-                          nullptr, {job->mp_grid[0], job->mp_grid[1], job->mp_grid[2]}};
-                rc = run_chunk<double>(ctx, kr, &jb, n_cta, 0.0, false, true, nullptr);
+                          nullptr, {job.mp_grid[0], job.mp_grid[1], job.mp_grid[2]}};
+                rc = run_chunk<double>(ctx, kr, &r.jb, r.n_cta, 0.0, false, true, nullptr);
                 if (rc) return rc;
             }
         }
     }
-    STAGE(ST_RED, launch_reduce(ctx->partials.as<double>(), n_cta, L.size(), ctx->out.as<double>(), ctx->stream));
+    STAGE(ST_RED, launch_reduce(ctx->partials.as<double>(), r.n_cta, L.size(), ctx->out.as<double>(), ctx->stream));
     std::vector<double> h(L.size());
     int hc[4] = {0, 0, 0, 0};
     CK(cudaMemcpyAsync(h.data(), ctx->out.p, L.size() * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaMemcpyAsync(hc, ctx->counters.p, 4 * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     ctx->d2h += L.size() * sizeof(double) + 4 * sizeof(int);
-    if (int r1 = stage_end(ctx, run_ev)) return r1;
+    if (int r1 = stage_end(ctx, r.run_ev)) return r1;
     CK(cudaStreamSynchronize(ctx->stream));
     CK(cudaGetLastError());
     if (ctx->tc.err) {
@@ -418,9 +476,9 @@ int run_impl(mepi_ctx* ctx, const mepi_job* job, mepi_acc* out) {
         CK(cudaMemcpy(&terr, ctx->tc.err, sizeof(int), cudaMemcpyDeviceToHost));
         if (terr) return MEPI_ERR_CUDA;
     }
-    rc = collect_timing(ctx, count);
+    rc = collect_timing(ctx, r.count);
     if (rc) return rc;
-    const int nE = job->n_eF, nv = job->valence_bands;
+    const int nE = job.n_eF, nv = job.valence_bands;
     auto put = [&](double* dst, int off, int n) {
         if (dst) std::memcpy(dst, h.data() + off, n * sizeof(double));
     };
@@ -432,18 +490,31 @@ int run_impl(mepi_ctx* ctx, const mepi_job* job, mepi_acc* out) {
     put(out->mep_ic, L.mic_off(), 9 * nv);
     put(out->mep_lc, L.mlc_off(), 9 * nv);
     put(out->mep_cs, L.mcs_off(), 9 * nv);
-    if (n_hw) {
-        put(out->velo_ahc, L.vah_off(), 18 * n_hw * nE);
-        put(out->kubo_ohc, L.koh_off(), 18 * n_hw * nE);
+    if (r.n_hw) {
+        put(out->velo_ahc, L.vah_off(), 18 * r.n_hw * nE);
+        put(out->kubo_ohc, L.koh_off(), 18 * r.n_hw * nE);
     }
-    out->n_k_done = count;
-    out->n_k_fp64 = fp64 ? count : (int64_t)redo.size();
+    out->n_k_done = r.count;
+    out->n_k_fp64 = r.fp64 ? r.count : (int64_t)redo.size();
     out->eig_max_sweeps = hc[0];
     // counters[1] counts FP64 Jacobi launches that hit the sweep cap (an error);
     // FP32 cap hits (counters[2]) were flagged and rerun in FP64.
     if (hc[1] > 0) return MEPI_ERR_EIG;
     return MEPI_OK;
 }
+
+int run_impl(mepi_ctx* ctx, const mepi_job* job, mepi_acc* out) {
+    int rc = run_prepare(ctx, job);
+    if (!rc) rc = run_enqueue(ctx);
+    if (!rc) rc = run_finish(ctx, out);
+    return rc;
+}
+
+// Process-wide record of tuned launch shapes, keyed by (device, N, nR, blocks).
+std::mutex g_tune_mu;
+std::map<std::array<int, 4>, mepi_tuning> g_tune;
+
+std::array<int, 4> tune_key(const mepi_ctx* c) { return {c->device, c->N, c->nR, c->nb}; }
 
 }  // namespace
 
@@ -583,6 +654,12 @@ int mepi_create(mepi_ctx** out, const mepi_model* m) {
     d.S = ctx->S.as<cplx<double>>();
     d.R = ctx->R.as<double>();
     d.tau = m->wf_centers ? ctx->tau.as<double>() : nullptr;
+    {
+        // launch shapes tuned earlier in this process for the same kind of model
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_tune.find(tune_key(ctx));
+        if (it != g_tune.end()) ctx->tune = it->second;
+    }
     *out = ctx;
     return MEPI_OK;
 }
@@ -713,6 +790,145 @@ int mepi_get_timing(const mepi_ctx* ctx, mepi_timing* t) {
     if (!ctx || !t) return MEPI_ERR_ARG;
     *t = ctx->timing;
     return MEPI_OK;
+}
+
+int mepi_set_tuning(mepi_ctx* ctx, const mepi_tuning* t) {
+    if (!ctx || !t || t->jacobi_threads < 0 || t->jacobi_kblock < 0 || t->chunk_k < 0) return MEPI_ERR_ARG;
+    if (t->jacobi_threads && (t->jacobi_threads % 32 || t->jacobi_threads > 256)) return MEPI_ERR_ARG;
+    ctx->tune = *t;
+    return MEPI_OK;
+}
+
+int mepi_get_tuning(const mepi_ctx* ctx, mepi_tuning* t) {
+    if (!ctx || !t) return MEPI_ERR_ARG;
+    *t = ctx->tune;
+    return MEPI_OK;
+}
+
+int mepi_autotune(mepi_ctx* ctx, const mepi_job* job, int64_t sample_k, mepi_tuning* best) {
+    if (!ctx || !job) return MEPI_ERR_ARG;
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return MEPI_ERR_CUDA;
+    try {
+        mepi_job j = *job;
+        j.k_begin = 0;
+        j.k_stride = 1;
+        j.k_count = sample_k > 0 ? sample_k : 32768;
+        j.chunk_k = 0;
+        mepi_acc acc{};
+        const mepi_tuning saved = ctx->tune;
+        ctx->tune = mepi_tuning{};
+        int rc = run_impl(ctx, &j, &acc);   // builds the slabs; also a warm-up
+        if (rc) {
+            ctx->tune = saved;
+            return rc;
+        }
+        const int np = ctx->N <= 8 ? 8 : ctx->N <= 16 ? 16 : ctx->N <= 32 ? 32 : 64;
+        mepi_tuning win{};
+        double best_ms = 1e300;
+        for (int threads : {64, 128, 256}) {
+            if (threads < np / 2) continue;
+            for (int kb : {4, 8, 16})
+                for (int64_t ch : {(int64_t)16384, (int64_t)65536}) {
+                    ctx->tune = mepi_tuning{threads, kb, ch, 0.0};
+                    rc = run_impl(ctx, &j, &acc);
+                    if (rc) {
+                        ctx->tune = saved;
+                        return rc;
+                    }
+                    const double ms = ctx->timing.run_ms;
+                    if (ms < best_ms) {
+                        best_ms = ms;
+                        win = ctx->tune;
+                        win.k_per_s = (double)acc.n_k_done / (ms * 1e-3);
+                    }
+                }
+        }
+        ctx->tune = win;
+        {
+            std::lock_guard<std::mutex> lk(g_tune_mu);
+            g_tune[tune_key(ctx)] = win;
+        }
+        if (best) *best = win;
+        return MEPI_OK;
+    } catch (const std::bad_alloc&) {
+        return MEPI_ERR_NOMEM;
+    } catch (...) {
+        return MEPI_ERR_CUDA;
+    }
+}
+
+int mepi_run_batch(int32_t n, mepi_ctx* const* ctxs, const mepi_job* jobs, mepi_acc* accs, double* graph_ms) {
+    if (n < 0 || (n > 0 && (!ctxs || !jobs || !accs))) return MEPI_ERR_ARG;
+    if (n == 0) return MEPI_OK;
+    for (int i = 0; i < n; ++i)
+        if (!ctxs[i] || ctxs[i]->device != ctxs[0]->device) return MEPI_ERR_ARG;
+    for (int i = 0; i < n; ++i)
+        for (int j = 0; j < i; ++j)
+            if (ctxs[i] == ctxs[j]) return MEPI_ERR_ARG;   // one run per context
+    if (cudaSetDevice(ctxs[0]->device) != cudaSuccess) return MEPI_ERR_CUDA;
+    cudaStream_t bs = nullptr;
+    cudaEvent_t fork = nullptr, t0 = nullptr, t1 = nullptr;
+    std::vector<cudaEvent_t> join(n, nullptr);
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    auto cleanup = [&](int rc) {
+        for (int i = 0; i < n; ++i) ctxs[i]->timed = true;
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        for (cudaEvent_t e : join)
+            if (e) cudaEventDestroy(e);
+        if (fork) cudaEventDestroy(fork);
+        if (t0) cudaEventDestroy(t0);
+        if (t1) cudaEventDestroy(t1);
+        if (bs) cudaStreamDestroy(bs);
+        return rc;
+    };
+    try {
+        // 1. prepare every context (allocations, slabs, k lists), outside the capture
+        for (int i = 0; i < n; ++i) {
+            ctxs[i]->timed = false;
+            int rc = run_prepare(ctxs[i], &jobs[i]);
+            if (rc) return cleanup(rc);
+        }
+        for (int i = 0; i < n; ++i)
+            if (cudaStreamSynchronize(ctxs[i]->stream) != cudaSuccess) return cleanup(MEPI_ERR_CUDA);
+        if (cudaStreamCreateWithFlags(&bs, cudaStreamNonBlocking) != cudaSuccess) return cleanup(MEPI_ERR_CUDA);
+        if (cudaEventCreateWithFlags(&fork, cudaEventDisableTiming) != cudaSuccess) return cleanup(MEPI_ERR_CUDA);
+        for (int i = 0; i < n; ++i)
+            if (cudaEventCreateWithFlags(&join[i], cudaEventDisableTiming) != cudaSuccess) return cleanup(MEPI_ERR_CUDA);
+        // 2. capture every context's chunk pipeline on its own stream into one graph
+        if (cudaStreamBeginCapture(bs, cudaStreamCaptureModeRelaxed) != cudaSuccess) return cleanup(MEPI_ERR_CUDA);
+        int rc = cudaEventRecord(fork, bs) == cudaSuccess ? 0 : MEPI_ERR_CUDA;
+        for (int i = 0; i < n && !rc; ++i) {
+            if (cudaStreamWaitEvent(ctxs[i]->stream, fork, 0) != cudaSuccess) { rc = MEPI_ERR_CUDA; break; }
+            rc = run_enqueue(ctxs[i]);
+            if (!rc && (cudaEventRecord(join[i], ctxs[i]->stream) != cudaSuccess ||
+                        cudaStreamWaitEvent(bs, join[i], 0) != cudaSuccess))
+                rc = MEPI_ERR_CUDA;
+        }
+        const cudaError_t ec = cudaStreamEndCapture(bs, &graph);
+        if (rc) return cleanup(rc);
+        if (ec != cudaSuccess || !graph) return cleanup(MEPI_ERR_CUDA);
+        if (cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess) return cleanup(MEPI_ERR_CUDA);
+        // 3. one launch
+        if (cudaEventCreate(&t0) != cudaSuccess || cudaEventCreate(&t1) != cudaSuccess) return cleanup(MEPI_ERR_CUDA);
+        if (cudaEventRecord(t0, bs) != cudaSuccess || cudaGraphLaunch(exec, bs) != cudaSuccess ||
+            cudaEventRecord(t1, bs) != cudaSuccess || cudaStreamSynchronize(bs) != cudaSuccess)
+            return cleanup(MEPI_ERR_CUDA);
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, t0, t1) != cudaSuccess) return cleanup(MEPI_ERR_CUDA);
+        if (graph_ms) *graph_ms = ms;
+        // 4. reruns, reductions and copies back, per context
+        for (int i = 0; i < n; ++i) {
+            rc = run_finish(ctxs[i], &accs[i]);
+            if (rc) return cleanup(rc);
+        }
+        return cleanup(MEPI_OK);
+    } catch (const std::bad_alloc&) {
+        return cleanup(MEPI_ERR_NOMEM);
+    } catch (...) {
+        return cleanup(MEPI_ERR_CUDA);
+    }
 }
 
 int mepi_destroy(mepi_ctx* ctx) {

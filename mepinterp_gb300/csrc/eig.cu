@@ -275,13 +275,15 @@ __global__ void __launch_bounds__(256) jacobi_kernel(int N, int64_t nk, int kblo
 template <typename T>
 cudaError_t launch_eig(int N, int64_t nk, const cplx<T>* W, int nbW, const cplx<double>* H64, T* E, cplx<T>* U,
                        int max_sweeps, int* sweeps_max, int* flag_cap, double degen_gap, int* redo_flag,
-                       cudaStream_t s) {
+                       cudaStream_t s, int threads_req, int kblock_req) {
     if (nk <= 0) return cudaSuccess;
     // a run of consecutive k-points per CTA, each warm-started from its
     // neighbour's eigenvectors (consecutive k-points are mesh neighbours)
-    const int kblock = 8;
+    const int kblock = kblock_req > 0 ? kblock_req : 8;
     const unsigned grid = (unsigned)((nk + kblock - 1) / kblock);
     auto go = [&](auto kern, int NP, int threads) {
+        // a tuned thread count: a multiple of 32, at least one thread per pair, at most 256
+        if (threads_req >= NP / 2 && threads_req <= 256 && threads_req % 32 == 0) threads = threads_req;
         const size_t smem = 6 * (size_t)NP * (NP + 1) * sizeof(T);
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e == cudaSuccess)
@@ -499,8 +501,8 @@ cudaError_t launch_refine(int N, int64_t nk, const cplx<double>* H64, const floa
 }
 
 template cudaError_t launch_eig<double>(int, int64_t, const cplx<double>*, int, const cplx<double>*, double*,
-                                        cplx<double>*, int, int*, int*, double, int*, cudaStream_t);
+                                        cplx<double>*, int, int*, int*, double, int*, cudaStream_t, int, int);
 template cudaError_t launch_eig<float>(int, int64_t, const cplx<float>*, int, const cplx<double>*, float*,
-                                       cplx<float>*, int, int*, int*, double, int*, cudaStream_t);
+                                       cplx<float>*, int, int*, int*, double, int*, cudaStream_t, int, int);
 
 }  // namespace mepi

@@ -29,7 +29,8 @@ def header_functions():
 
 def test_exports_every_declared_symbol(lib):
     names = header_functions()
-    assert {"mepi_create", "mepi_run", "mepi_destroy", "mepi_strerror", "mepi_interp_k"} <= set(names)
+    assert {"mepi_create", "mepi_run", "mepi_destroy", "mepi_strerror", "mepi_interp_k", "mepi_run_batch",
+            "mepi_autotune"} <= set(names)
     for n in names:
         assert hasattr(lib, n), n
 
@@ -37,7 +38,7 @@ def test_exports_every_declared_symbol(lib):
 def test_struct_layouts_match_header(tmp_path):
     """sizeof/offsetof from a C compile of mepi.h equal the ctypes mirror's."""
     fields = {"mepi_model": api.MepiModel, "mepi_job": api.MepiJob, "mepi_acc": api.MepiAcc,
-              "mepi_timing": api.MepiTiming}
+              "mepi_timing": api.MepiTiming, "mepi_tuning": api.MepiTuning}
     src = ['#include <stdio.h>', '#include <stddef.h>', '#include "mepi.h"', "int main(void){"]
     for cname, cls in fields.items():
         src.append(f'printf("{cname} %zu\\n", sizeof({cname}));')
