@@ -107,6 +107,10 @@ typedef struct {
     const double *hw_lst;      /* hw_lst(n_hw), Hartree ([Laser] get_linspace) */
     double eta_smr;            /* [Fermi] eta_smearing, Hartree: the reference's
                                   i_eta_smr = i * eta_smr */
+    const int64_t *k_list;     /* optional: k_count 0-based linear mesh indices
+                                  (kx fastest) to run instead of k_begin,
+                                  k_stride -- e.g. the cells an adaptive
+                                  refinement picked; NULL = the stride rule */
 } mepi_job;
 
 /* Unnormalised local sums, like the reference's *_loc arrays
@@ -128,6 +132,11 @@ typedef struct {
                                   complex, as (re, im) pairs */
     double *kubo_ohc;          /* MEPI_OUT_OPT_HALL: kubo_ohc_loc(3,3,n_hw,n_eF)
                                   complex, as (re, im) pairs */
+    double *perk;              /* optional per-k output, perk(4, n_k) in the
+                                  job's k order: the (y,z), (z,x), (x,y)
+                                  entries of the k-point's kubo_ahc_tens term
+                                  at ef_lst(1), and the band gap across
+                                  ef_lst(1) (Hartree) */
 } mepi_acc;
 
 /* Device time of each stage of the last mepi_run (CUDA events on the
@@ -186,13 +195,22 @@ int mepi_autotune(mepi_ctx *ctx, const mepi_job *job, int64_t sample_k, mepi_tun
 int mepi_set_tuning(mepi_ctx *ctx, const mepi_tuning *t);
 int mepi_get_tuning(const mepi_ctx *ctx, mepi_tuning *t);
 
+/* Device-memory limit of a context (no counterpart in the reference; 0, the
+ * default, = half the free memory for the separable Fourier slabs and 8 GB --
+ * 3 GB in the FP64 form -- for the per-chunk buffers).  With a limit, both
+ * take at most half of it each: the chunk shrinks, and the slabs of a large
+ * mesh are built for one range of qx after the other during the run.
+ * Results do not depend on the limit. */
+int mepi_set_mem_limit(mepi_ctx *ctx, uint64_t bytes);
+
 /* Batched form.  No counterpart in the reference, where each model is a
  * separate run.  n (context, job) pairs -- models of different band and R
  * counts, each with its own mesh, Fermi sweep and precision -- run as ONE
  * CUDA graph: every context's chunk pipeline is captured on its own stream
  * (independent models overlap on the GPU) and the graph is launched once.
  * The FP64 reruns of the mixed form, the reductions and the copies back
- * follow per context.  All contexts must be on the same device.  graph_ms
+ * follow per context.  The contexts share 80% of the free device memory
+ * (each within its own mepi_set_mem_limit as well).  All contexts must be on the same device.  graph_ms
  * (optional) receives the device time of the graph launch.  Results equal
  * those of n separate mepi_run calls. */
 int mepi_run_batch(int32_t n, mepi_ctx *const *ctxs, const mepi_job *jobs, mepi_acc *accs, double *graph_ms);

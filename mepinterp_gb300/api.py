@@ -53,7 +53,7 @@ class MepiJob(C.Structure):
                 ("k_count", C.c_int64), ("n_eF", C.c_int32), ("ef_lst", C.c_void_p),
                 ("T_kelvin", C.c_double), ("valence_bands", C.c_int32), ("outputs", C.c_uint32),
                 ("precision", C.c_int32), ("chunk_k", C.c_int64), ("degen_gap", C.c_double),
-                ("n_hw", C.c_int32), ("hw_lst", C.c_void_p), ("eta_smr", C.c_double)]
+                ("n_hw", C.c_int32), ("hw_lst", C.c_void_p), ("eta_smr", C.c_double), ("k_list", C.c_void_p)]
 
 
 class MepiAcc(C.Structure):
@@ -61,7 +61,7 @@ class MepiAcc(C.Structure):
                 ("mep_ic", C.c_void_p), ("mep_lc", C.c_void_p), ("mep_cs", C.c_void_p),
                 ("kubo_mep_ic", C.c_void_p), ("kubo_mep_lc", C.c_void_p), ("kubo_mep_cs", C.c_void_p),
                 ("n_k_done", C.c_int64), ("n_k_fp64", C.c_int64), ("eig_max_sweeps", C.c_int32),
-                ("velo_ahc", C.c_void_p), ("kubo_ohc", C.c_void_p)]
+                ("velo_ahc", C.c_void_p), ("kubo_ohc", C.c_void_p), ("perk", C.c_void_p)]
 
 
 STAGES = ("ft", "phase", "fth", "eig", "refine", "rot", "gauge", "bandsum", "reduce")
@@ -100,6 +100,8 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
     lib.mepi_autotune.restype = C.c_int
     lib.mepi_set_tuning.argtypes = [P, C.POINTER(MepiTuning)]
     lib.mepi_set_tuning.restype = C.c_int
+    lib.mepi_set_mem_limit.argtypes = [P, C.c_uint64]
+    lib.mepi_set_mem_limit.restype = C.c_int
     lib.mepi_get_tuning.argtypes = [P, C.POINTER(MepiTuning)]
     lib.mepi_get_tuning.restype = C.c_int
     lib.mepi_run_batch.argtypes = [C.c_int32, C.POINTER(P), C.POINTER(MepiJob), C.POINTER(MepiAcc),
@@ -187,17 +189,21 @@ class Context:
 
     # ------------------------------------------------------------------
     def core_worker_loc(self, job: dict, precision: int = PREC_FP64, k_begin: int = 0, k_stride: int = 1,
-                        k_count: int = -1, chunk_k: int = 0, degen_gap: float = -1.0) -> dict:
-        """k-loop body of src/core.f90:165-270 for k = k_begin + s*k_stride.
+                        k_count: int = -1, chunk_k: int = 0, degen_gap: float = -1.0, k_list=None,
+                        perk: bool = False) -> dict:
+        """k-loop body of src/core.f90:165-270 for k = k_begin + s*k_stride
+        (or for the mesh indices ``k_list``).
 
         ``job`` keys: mp_grid, ef_lst (Hartree), T_kelvin, valence_bands and
         optionally do_ahc / do_mep / do_kubo (default True), and hw_lst
         (Hartree) with eta_smr for the optical Hall tensors velo_ahc and
         kubo_ohc (3,3,n_hw,n_eF) that the reference computes with do_ahc.
         Returns the unnormalised local sums with the reference's shapes
-        (Fortran order).
+        (Fortran order); with ``perk`` also "perk" (n_k, 4): per k-point the
+        (y,z), (z,x), (x,y) entries of its AHC term at ef_lst[0] and the band
+        gap across ef_lst[0].
         """
-        call = _JobCall(job, precision, k_begin, k_stride, k_count, chunk_k, degen_gap)
+        call = _JobCall(job, precision, k_begin, k_stride, k_count, chunk_k, degen_gap, k_list, perk)
         _check(self.lib.mepi_run(self._h, C.byref(call.j), C.byref(call.acc)))
         return call.result()
 
@@ -218,6 +224,12 @@ class Context:
     def set_tuning(self, jacobi_threads: int = 0, jacobi_kblock: int = 0, chunk_k: int = 0) -> None:
         t = MepiTuning(int(jacobi_threads), int(jacobi_kblock), int(chunk_k), 0.0)
         _check(self.lib.mepi_set_tuning(self._h, C.byref(t)))
+
+    def set_mem_limit(self, nbytes: int) -> None:
+        """Device-memory limit for the separable slabs and chunk buffers (0 =
+        the defaults); a large mesh under a small limit builds its slabs one
+        qx range at a time.  Results do not depend on it."""
+        _check(self.lib.mepi_set_mem_limit(self._h, int(nbytes)))
 
     def get_wann_interp(self, kpts, precision: int = PREC_FP64):
         """en_k (nk,N), V (nk,3,N,N), A_diag (nk,3,N), Om_diag (nk,3,3,N) in C order."""
@@ -250,7 +262,7 @@ class _JobCall:
     """A mepi_job and its mepi_acc with the result arrays they point to."""
 
     def __init__(self, job: dict, precision: int = PREC_FP64, k_begin: int = 0, k_stride: int = 1,
-                 k_count: int = -1, chunk_k: int = 0, degen_gap: float = -1.0):
+                 k_count: int = -1, chunk_k: int = 0, degen_gap: float = -1.0, k_list=None, perk: bool = False):
         self.ef = np.ascontiguousarray(np.atleast_1d(np.asarray(job["ef_lst"], np.float64)))
         nE = self.ef.size
         nv = int(job["valence_bands"])
@@ -258,6 +270,15 @@ class _JobCall:
         for i in range(3):
             j.mp_grid[i] = int(job["mp_grid"][i])
         j.k_begin, j.k_stride, j.k_count = int(k_begin), int(k_stride), int(k_count)
+        self.k_list = None
+        n_tot = int(np.prod([int(x) for x in job["mp_grid"]]))
+        if k_list is not None:
+            self.k_list = np.ascontiguousarray(np.asarray(k_list, np.int64).ravel())
+            j.k_list, j.k_count, j.k_begin, j.k_stride = self.k_list.ctypes.data, self.k_list.size, 0, 1
+            n_k = self.k_list.size
+        else:
+            owned = max(0, -(-(n_tot - int(k_begin)) // int(k_stride))) if int(k_stride) > 0 else 0
+            n_k = owned if int(k_count) < 0 else min(int(k_count), owned)
         j.n_eF, j.ef_lst = nE, self.ef.ctypes.data
         j.T_kelvin = float(job.get("T_kelvin", 0.0))
         j.valence_bands = nv
@@ -286,6 +307,8 @@ class _JobCall:
         if outs & OUT_OPT_HALL:
             self.res["velo_ahc"] = np.zeros((3, 3, self.hw.size, nE), np.complex128, order="F")
             self.res["kubo_ohc"] = np.zeros((3, 3, self.hw.size, nE), np.complex128, order="F")
+        if perk:
+            self.res["perk"] = np.zeros((n_k, 4))
         self.acc = MepiAcc()
         for key, arr in self.res.items():
             setattr(self.acc, key, arr.ctypes.data if arr.size else None)

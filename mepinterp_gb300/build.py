@@ -19,7 +19,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libmepi_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["capi.cu", "ft.cu", "ft_tc.cu", "ft_sep.cu", "eig.cu", "rot.cu", "gauge.cu", "bandsum.cu"]
+SOURCES = ["capi.cu", "ft.cu", "ft_tc.cu", "ft_sep.cu", "eig.cu", "rot.cu", "gauge.cu", "bandsum.cu", "mlp.cu"]
 
 
 def _nvcc() -> str:
@@ -40,7 +40,8 @@ def build(force: bool = False, verbose: bool = False) -> str:
     nvcc = _nvcc()
     os.makedirs(BUILD, exist_ok=True)
     headers = [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".cuh", ".h"))]
-    headers.append(os.path.join(HERE, "..", "include", "mepi.h"))
+    inc = os.path.join(HERE, "..", "include")
+    headers += [os.path.join(inc, h) for h in os.listdir(inc) if h.endswith(".h")]
     srcs = [s for s in SOURCES if os.path.exists(os.path.join(CSRC, s))]
     objs = []
     jobs = []

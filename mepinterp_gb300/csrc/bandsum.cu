@@ -539,6 +539,71 @@ template cudaError_t launch_opt_hall<double>(const DevModel&, const JobDev&, int
 template cudaError_t launch_opt_hall<float>(const DevModel&, const JobDev&, int64_t, const double*,
                                             const cplx<float>*, const int*, double*, int, cudaStream_t);
 
+// Per-k AHC integrand at one Fermi energy and the band gap there (inputs of
+// the adaptive refinement).  out[pos][0..2] = the (y,z), (z,x), (x,y) entries
+// of the term kubo_ahc_tens adds for this k (src/kubo.f90:37-78),
+//     -sum_n f_n curv_n(i,j) = 2 sum_{n<m} (f_n - f_m) Im(V_i,nm V_j,mn) / (E_m - E_n)^2
+// (the (n,m) and (m,n) terms of the reference's double sum are equal and
+// opposite, so the pair form drops the occupied-occupied cancellation), and
+// out[pos][3] = E_c - E_v across the Fermi energy (twice the distance to the
+// nearest band when it lies outside all bands).  One warp per k-point.
+template <typename T>
+__global__ void __launch_bounds__(256) perk_kernel(int N, int64_t nk, const double* __restrict__ E,
+                                                   const cplx<T>* __restrict__ V, double ef, double T_kelvin,
+                                                   const int64_t* __restrict__ pos, int64_t pos0,
+                                                   double* __restrict__ out) {
+    const int lane = threadIdx.x & 31;
+    const int64_t k = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (k >= nk) return;
+    const double* Ek = E + (size_t)k * N;
+    const size_t NN = (size_t)N * N;
+    const cplx<T>* Vk = V + (size_t)k * 3 * NN;
+    double acc[3] = {0.0, 0.0, 0.0};
+    for (int n = 0; n < N; ++n) {
+        const double fn = fd_stat<double>(Ek[n], ef, T_kelvin);
+        for (int m = n + 1 + lane; m < N; m += 32) {
+            const double w = fn - fd_stat<double>(Ek[m], ef, T_kelvin);
+            if (w == 0.0) continue;
+            const double d = Ek[m] - Ek[n];
+            const double c = 2.0 * w / (d * d);
+            cplx<T> a[3], b[3];
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+                a[i] = Vk[i * NN + (size_t)n * N + m];
+                b[i] = Vk[i * NN + (size_t)m * N + n];
+            }
+            // Im(V_i,nm V_j,mn) for (i,j) = (y,z), (z,x), (x,y)
+            acc[0] += c * (double)(a[1] * b[2]).im;
+            acc[1] += c * (double)(a[2] * b[0]).im;
+            acc[2] += c * (double)(a[0] * b[1]).im;
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < 3; ++i) acc[i] = warp_sum(acc[i]);
+    if (lane == 0) {
+        int nF = 0;
+        while (nF < N && Ek[nF] < ef) ++nF;
+        const double gap = nF == 0 ? 2.0 * (Ek[0] - ef) : nF == N ? 2.0 * (ef - Ek[N - 1]) : Ek[nF] - Ek[nF - 1];
+        double* o = out + 4 * (size_t)(pos ? pos[k] : pos0 + k);
+        o[0] = acc[0];
+        o[1] = acc[1];
+        o[2] = acc[2];
+        o[3] = gap;
+    }
+}
+
+template <typename T>
+cudaError_t launch_perk(int N, int64_t nk, const double* E, const cplx<T>* V, double ef, double T_kelvin,
+                        const int64_t* pos, int64_t pos0, double* out, cudaStream_t s) {
+    if (nk <= 0) return cudaSuccess;
+    perk_kernel<T><<<(unsigned)((nk + 7) / 8), 256, 0, s>>>(N, nk, E, V, ef, T_kelvin, pos, pos0, out);
+    return cudaGetLastError();
+}
+template cudaError_t launch_perk<double>(int, int64_t, const double*, const cplx<double>*, double, double,
+                                         const int64_t*, int64_t, double*, cudaStream_t);
+template cudaError_t launch_perk<float>(int, int64_t, const double*, const cplx<float>*, double, double,
+                                        const int64_t*, int64_t, double*, cudaStream_t);
+
 cudaError_t launch_reduce(const double* partials, int n_cta, int size, double* out, cudaStream_t s) {
     reduce_kernel<<<(size + 255) / 256, 256, 0, s>>>(partials, n_cta, size, out);
     return cudaGetLastError();

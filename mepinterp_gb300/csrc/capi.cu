@@ -70,6 +70,9 @@ struct mepi_ctx {
     DevBuf S, R, tau;
     // per-chunk work buffers
     DevBuf W, E, E64, H64, U, HA, OD, V, CSV, ODH, flags, klist, kpts, partials, out, counters;
+    // explicit k lists (mepi_job.k_list) and the per-k output (mepi_acc.perk)
+    DevBuf jlist, kpos, rpos, perk;
+    std::vector<int64_t> kpos_host;     // job position of each kcol_host entry
     int* h_flags = nullptr;  // pinned
     size_t h_flags_cap = 0;
     std::vector<StageEv> events;
@@ -86,6 +89,7 @@ struct mepi_ctx {
     // k-points of the run in (qx, qy)-column order, for slab reuse
     DevBuf kcol;
     std::vector<int64_t> kcol_host;
+    std::vector<int64_t> kslab;         // kcol_host index where each qx slab starts (+ the end)
     int64_t kcol_key[6] = {-1, -1, -1, -1, -1, -1};
     // launch shapes picked by mepi_autotune (0 = the built-in choice)
     mepi_tuning tune{};
@@ -99,8 +103,11 @@ struct mepi_ctx {
         AccLayout L{1, 0, 0};
         JobDev jb{};
         size_t run_ev = 0;
+        bool perk = false;              // per-k output requested
     } run;
     bool timed = true;                  // per-stage CUDA events (off inside a graph capture)
+    size_t mem_budget = 0;              // device bytes for slabs + chunk buffers (0: the defaults)
+    size_t mem_limit = 0;               // the caller's limit (mepi_set_mem_limit)
 };
 
 namespace {
@@ -178,6 +185,23 @@ int ensure_chunk(mepi_ctx* ctx, int64_t chunk) {
     CKM(ctx->CSV.ensure(chunk * N * sizeof(T)));
     CKM(ctx->flags.ensure(chunk * sizeof(int)));
     return 0;
+}
+
+// device bytes of a context's separable slabs and per-chunk buffers
+size_t run_buffer_bytes(const mepi_ctx* ctx) {
+    size_t b = ctx->sep.dev_bytes;
+    for (const DevBuf* d : {&ctx->W, &ctx->E, &ctx->E64, &ctx->H64, &ctx->U, &ctx->HA, &ctx->OD, &ctx->V, &ctx->CSV,
+                            &ctx->flags})
+        b += d->bytes;
+    return b;
+}
+
+void release_run_buffers(mepi_ctx* ctx) {
+    cudaStreamSynchronize(ctx->stream);
+    for (DevBuf* d : {&ctx->W, &ctx->E, &ctx->E64, &ctx->H64, &ctx->U, &ctx->HA, &ctx->OD, &ctx->V, &ctx->CSV,
+                      &ctx->flags})
+        d->release();
+    sep_plan_free(ctx->sep);
 }
 
 // One chunk of k-points through FT -> eig (-> FP64 refinement) -> rot ->
@@ -268,9 +292,12 @@ int collect_timing(mepi_ctx* ctx, int64_t nk) {
     return 0;
 }
 
-int64_t default_chunk(int N, int nb, bool fp64) {
+// k-points per chunk: the per-k buffers within 8 GB (3 GB for the FP64 form),
+// or within mem_budget / 2 when the context has a budget.
+int64_t default_chunk(int N, int nb, bool fp64, size_t mem_budget = 0) {
     size_t per = fp64 ? per_k_bytes<double>(N, nb) : per_k_bytes<float>(N, nb);
     size_t budget = fp64 ? ((size_t)3 << 30) : ((size_t)8 << 30);
+    if (mem_budget) budget = std::min(budget, mem_budget / 2);
     int64_t c = (int64_t)(budget / per);
     c = std::min<int64_t>(c, fp64 ? 16384 : 65536);
     c = std::max<int64_t>(64, c & ~(int64_t)63);
@@ -284,11 +311,14 @@ int prepare_sep(mepi_ctx* ctx, const mepi_job* job, int64_t count, bool fp64) {
     ctx->plan_ms = 0.0;
     if (ctx->ft_pref != 0 || count <= 0) return 0;
     const int mp[3] = {job->mp_grid[0], job->mp_grid[1], job->mp_grid[2]};
+    const size_t budget = ctx->mem_budget / 2;   // 0: half the free memory
     const bool reuse = ctx->sep.ready && ctx->sep.fp64 == fp64 && ctx->sep.mp[0] == mp[0] && ctx->sep.mp[1] == mp[1] &&
-                       ctx->sep.mp[2] == mp[2];
+                       ctx->sep.mp[2] == mp[2] && (budget == 0 || ctx->sep.dev_bytes <= budget);
     if (!reuse) {
         const auto t0 = std::chrono::steady_clock::now();
-        int rc = sep_plan_build(ctx->sep, ctx->dm, ctx->R_host.data(), ctx->S_host.data(), mp, fp64, ctx->stream);
+        sep_plan_free(ctx->sep);
+        int rc = sep_plan_build(ctx->sep, ctx->dm, ctx->R_host.data(), ctx->S_host.data(), mp, fp64, budget,
+                                ctx->stream);
         if (rc == 1) return 0;
         if (rc) {
             cudaGetLastError();
@@ -298,23 +328,54 @@ int prepare_sep(mepi_ctx* ctx, const mepi_job* job, int64_t count, bool fp64) {
         ctx->plan_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     }
     const int64_t key[6] = {mp[0], mp[1], mp[2], job->k_begin, job->k_stride, count};
-    if (!std::equal(key, key + 6, ctx->kcol_key)) {
+    if (job->k_list || !std::equal(key, key + 6, ctx->kcol_key)) {
         std::vector<int64_t> L;
         L.reserve(count);
         const int64_t M = (int64_t)mp[0] * mp[1];
-        for (int qx = 0; qx < mp[0]; ++qx)
-            for (int qy = 0; qy < mp[1]; ++qy)
-                for (int qz = 0; qz < mp[2]; ++qz) {
-                    const int64_t d = qx + (int64_t)mp[0] * qy + M * qz - job->k_begin;
-                    if (d >= 0 && d % job->k_stride == 0 && d / job->k_stride < count) L.push_back(d + job->k_begin);
-                }
+        if (job->k_list) {
+            // the caller's list, sorted into column order (positions kept for the per-k output)
+            auto col = [&](int64_t ki) {
+                const int64_t qx = ki % mp[0], qy = (ki / mp[0]) % mp[1], qz = ki / M;
+                return (qx * mp[1] + qy) * mp[2] + qz;
+            };
+            std::vector<int64_t> ord(count);
+            for (int64_t i = 0; i < count; ++i) ord[i] = i;
+            std::stable_sort(ord.begin(), ord.end(),
+                             [&](int64_t a, int64_t b) { return col(job->k_list[a]) < col(job->k_list[b]); });
+            for (int64_t i = 0; i < count; ++i) L.push_back(job->k_list[ord[i]]);
+            ctx->kpos_host.swap(ord);
+        } else {
+            for (int qx = 0; qx < mp[0]; ++qx)
+                for (int qy = 0; qy < mp[1]; ++qy)
+                    for (int qz = 0; qz < mp[2]; ++qz) {
+                        const int64_t d = qx + (int64_t)mp[0] * qy + M * qz - job->k_begin;
+                        if (d >= 0 && d % job->k_stride == 0 && d / job->k_stride < count)
+                            L.push_back(d + job->k_begin);
+                    }
+            ctx->kpos_host.resize(L.size());
+            for (size_t i = 0; i < L.size(); ++i) ctx->kpos_host[i] = (L[i] - job->k_begin) / job->k_stride;
+        }
         if ((int64_t)L.size() != count) return MEPI_ERR_ARG;
         CKM(ctx->kcol.ensure(L.size() * sizeof(int64_t)));
         CK(cudaMemcpyAsync(ctx->kcol.p, L.data(), L.size() * sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream));
         CK(cudaStreamSynchronize(ctx->stream));
         ctx->h2d += L.size() * sizeof(int64_t);
+        CKM(ctx->kpos.ensure(std::max<int64_t>(count, 1) * sizeof(int64_t)));
+        CK(cudaMemcpyAsync(ctx->kpos.p, ctx->kpos_host.data(), count * sizeof(int64_t), cudaMemcpyHostToDevice,
+                           ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
         ctx->kcol_host.swap(L);
         std::copy(key, key + 6, ctx->kcol_key);
+        if (job->k_list) std::fill(ctx->kcol_key, ctx->kcol_key + 6, -1);   // a list is never reused
+        ctx->kslab.clear();
+    }
+    // the list runs qx-outermost: each slab of nqx consecutive qx is one range of it
+    const int nslab = (mp[0] + ctx->sep.nqx - 1) / ctx->sep.nqx;
+    if ((int)ctx->kslab.size() != nslab + 1) {
+        ctx->kslab.assign(nslab + 1, count);
+        int j = 0;
+        for (int64_t i = 0; i < count && j < nslab; ++i)
+            while (j < nslab && (int)(ctx->kcol_host[i] % mp[0]) >= j * ctx->sep.nqx) ctx->kslab[j++] = i;
     }
     ctx->sep_active = true;
     return 0;
@@ -323,7 +384,7 @@ int prepare_sep(mepi_ctx* ctx, const mepi_job* job, int64_t count, bool fp64) {
 // Phase 1 of a run: validate, size and allocate, build the separable slabs and
 // the k list, upload the Fermi and photon energies.  Enqueues only small
 // copies and memsets on the context's stream.
-int run_prepare(mepi_ctx* ctx, const mepi_job* job) {
+int run_prepare(mepi_ctx* ctx, const mepi_job* job, const mepi_acc* out) {
     const int N = ctx->N;
     const int64_t nk_tot = (int64_t)job->mp_grid[0] * job->mp_grid[1] * job->mp_grid[2];
     if (job->mp_grid[0] <= 0 || job->mp_grid[1] <= 0 || job->mp_grid[2] <= 0) return MEPI_ERR_ARG;
@@ -337,11 +398,20 @@ int run_prepare(mepi_ctx* ctx, const mepi_job* job) {
         return MEPI_ERR_ARG;
     mepi_ctx::Run& r = ctx->run;
     r.job = *job;
-    const int64_t owned = job->k_begin < nk_tot ? (nk_tot - job->k_begin + job->k_stride - 1) / job->k_stride : 0;
-    r.count = job->k_count < 0 ? owned : std::min<int64_t>(job->k_count, owned);
+    if (job->k_list) {
+        if (job->k_count < 0) return MEPI_ERR_ARG;
+        for (int64_t i = 0; i < job->k_count; ++i)
+            if (job->k_list[i] < 0 || job->k_list[i] >= nk_tot) return MEPI_ERR_ARG;
+        r.count = job->k_count;
+    } else {
+        const int64_t owned =
+            job->k_begin < nk_tot ? (nk_tot - job->k_begin + job->k_stride - 1) / job->k_stride : 0;
+        r.count = job->k_count < 0 ? owned : std::min<int64_t>(job->k_count, owned);
+    }
+    r.perk = out && out->perk;
     r.fp64 = job->precision == MEPI_PREC_FP64;
     int64_t chunk = job->chunk_k > 0 ? job->chunk_k
-                  : ctx->tune.chunk_k > 0 ? ctx->tune.chunk_k : default_chunk(N, ctx->nb, r.fp64);
+                  : ctx->tune.chunk_k > 0 ? ctx->tune.chunk_k : default_chunk(N, ctx->nb, r.fp64, ctx->mem_budget);
     r.chunk = std::max<int64_t>(1, std::min<int64_t>(chunk, std::max<int64_t>(r.count, 1)));
     r.degen_gap = job->degen_gap >= 0 ? job->degen_gap : 3e-3;
     r.n_hw = opt_hall ? job->n_hw : 0;
@@ -375,6 +445,12 @@ int run_prepare(mepi_ctx* ctx, const mepi_job* job) {
     jb.nW = r.n_hw;
     jb.hw = r.n_hw ? d_hw : nullptr;
     jb.eta = job->eta_smr;
+    if (job->k_list && r.count > 0) {
+        CKM(ctx->jlist.ensure(r.count * sizeof(int64_t)));
+        CK(cudaMemcpyAsync(ctx->jlist.p, job->k_list, r.count * sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream));
+        ctx->h2d += r.count * sizeof(int64_t);
+    }
+    if (r.perk) CKM(ctx->perk.ensure(std::max<int64_t>(r.count, 1) * 4 * sizeof(double)));
     int rc = prepare_sep(ctx, job, r.count, r.fp64);
     if (rc) return rc;
     rc = r.fp64 ? ensure_chunk<double>(ctx, r.chunk) : ensure_chunk<float>(ctx, r.chunk);
@@ -407,22 +483,58 @@ KRange chunk_range(const mepi_ctx* ctx, int64_t c0, int64_t cn) {
     if (ctx->sep_active)
         return KRange{0, 1, cn, const_cast<mepi_ctx*>(ctx)->kcol.as<int64_t>() + c0, nullptr,
                       {job.mp_grid[0], job.mp_grid[1], job.mp_grid[2]}};
+    if (job.k_list)
+        return KRange{0, 1, cn, const_cast<mepi_ctx*>(ctx)->jlist.as<int64_t>() + c0, nullptr,
+                      {job.mp_grid[0], job.mp_grid[1], job.mp_grid[2]}};
     return KRange{job.k_begin + c0 * job.k_stride, job.k_stride, cn, nullptr, nullptr,
                   {job.mp_grid[0], job.mp_grid[1], job.mp_grid[2]}};
+}
+
+int enqueue_range(mepi_ctx* ctx, int64_t b, int64_t e);
+
+// per-k AHC integrand and gap of the chunk just run (its energies and velocities
+// are still in the chunk buffers)
+template <typename T>
+int enqueue_perk(mepi_ctx* ctx, int64_t cn, const int64_t* pos, int64_t pos0) {
+    const mepi_ctx::Run& r = ctx->run;
+    STAGE(ST_BAND, launch_perk<T>(ctx->N, cn, ctx->E64.as<double>(), ctx->V.as<cplx<T>>(), r.job.ef_lst[0],
+                                  r.job.T_kelvin, pos, pos0, ctx->perk.as<double>(), ctx->stream));
+    return 0;
 }
 
 // Phase 2: every chunk of the run, as stream work only (no allocation, no
 // synchronisation), so that it can be captured into a CUDA graph.
 int run_enqueue(mepi_ctx* ctx) {
     mepi_ctx::Run& r = ctx->run;
+    if (ctx->sep_active && !ctx->sep.whole()) {
+        // one qx slab after the other: build its sums, then run its chunks
+        for (size_t j = 0; j + 1 < ctx->kslab.size(); ++j) {
+            const int64_t s0 = ctx->kslab[j], s1 = ctx->kslab[j + 1];
+            if (s1 <= s0) continue;
+            const int qx0 = (int)j * ctx->sep.nqx;
+            if (ctx->sep.built_qx0 != qx0) STAGE(ST_FT, launch_sep_slab(ctx->sep, qx0, ctx->stream));
+            if (int rc = enqueue_range(ctx, s0, s1)) return rc;
+        }
+        return 0;
+    }
+    return enqueue_range(ctx, 0, r.count);
+}
+
+// the chunks of run k-points [b, e)
+int enqueue_range(mepi_ctx* ctx, int64_t b, int64_t e) {
+    mepi_ctx::Run& r = ctx->run;
     int rc = 0;
-    for (int64_t c0 = 0; c0 < r.count; c0 += r.chunk) {
-        const int64_t cn = std::min(r.chunk, r.count - c0);
+    for (int64_t c0 = b; c0 < e; c0 += r.chunk) {
+        const int64_t cn = std::min(r.chunk, e - c0);
         const KRange kr = chunk_range(ctx, c0, cn);
+        // job positions of the chunk's k-points for the per-k output
+        const int64_t* pos = ctx->sep_active ? ctx->kpos.as<int64_t>() + c0 : nullptr;
         if (r.fp64) {
             rc = run_chunk<double>(ctx, kr, &r.jb, r.n_cta, 0.0, false, true, nullptr);
+            if (!rc && r.perk) rc = enqueue_perk<double>(ctx, cn, pos, c0);
         } else {
             rc = run_chunk<float>(ctx, kr, &r.jb, r.n_cta, r.degen_gap, true, true, nullptr);
+            if (!rc && r.perk) rc = enqueue_perk<float>(ctx, cn, pos, c0);
             if (!rc) {
                 CK(cudaMemcpyAsync(ctx->h_flags + c0, ctx->flags.p, cn * sizeof(int), cudaMemcpyDeviceToHost,
                                    ctx->stream));
@@ -440,27 +552,43 @@ int run_finish(mepi_ctx* ctx, mepi_acc* out) {
     mepi_ctx::Run& r = ctx->run;
     const mepi_job& job = r.job;
     const AccLayout& L = r.L;
-    std::vector<int64_t> redo;
+    std::vector<int64_t> redo, redo_pos;
     int rc = 0;
     if (!r.fp64) {
         CK(cudaStreamSynchronize(ctx->stream));
         for (int64_t i = 0; i < r.count; ++i)
-            if (ctx->h_flags[i]) redo.push_back(ctx->sep_active ? ctx->kcol_host[i] : job.k_begin + i * job.k_stride);
+            if (ctx->h_flags[i]) {
+                redo.push_back(ctx->sep_active ? ctx->kcol_host[i]
+                               : job.k_list    ? job.k_list[i]
+                                               : job.k_begin + i * job.k_stride);
+                redo_pos.push_back(ctx->sep_active ? ctx->kpos_host[i] : i);
+            }
+        // a slabbed plan holds only its last slab: the reruns take the direct sums
+        const bool sep_keep = ctx->sep_active;
+        if (!ctx->sep.whole()) ctx->sep_active = false;
         if (!redo.empty()) {
-            int64_t rchunk = std::min<int64_t>(default_chunk(ctx->N, ctx->nb, true), (int64_t)redo.size());
+            int64_t rchunk =
+                std::min<int64_t>(default_chunk(ctx->N, ctx->nb, true, ctx->mem_budget), (int64_t)redo.size());
             rc = ensure_chunk<double>(ctx, rchunk);
             if (rc) return rc;
             CKM(ctx->klist.ensure(redo.size() * sizeof(int64_t)));
             CK(cudaMemcpyAsync(ctx->klist.p, redo.data(), redo.size() * sizeof(int64_t), cudaMemcpyHostToDevice,
                                ctx->stream));
             ctx->h2d += redo.size() * sizeof(int64_t);
+            if (r.perk) {
+                CKM(ctx->rpos.ensure(redo_pos.size() * sizeof(int64_t)));
+                CK(cudaMemcpyAsync(ctx->rpos.p, redo_pos.data(), redo_pos.size() * sizeof(int64_t),
+                                   cudaMemcpyHostToDevice, ctx->stream));
+            }
             for (int64_t c0 = 0; c0 < (int64_t)redo.size(); c0 += rchunk) {
                 KRange kr{0, 1, std::min<int64_t>(rchunk, (int64_t)redo.size() - c0), ctx->klist.as<int64_t>() + c0,
                           nullptr, {job.mp_grid[0], job.mp_grid[1], job.mp_grid[2]}};
                 rc = run_chunk<double>(ctx, kr, &r.jb, r.n_cta, 0.0, false, true, nullptr);
+                if (!rc && r.perk) rc = enqueue_perk<double>(ctx, kr.count, ctx->rpos.as<int64_t>() + c0, 0);
                 if (rc) return rc;
             }
         }
+        ctx->sep_active = sep_keep;
     }
     STAGE(ST_RED, launch_reduce(ctx->partials.as<double>(), r.n_cta, L.size(), ctx->out.as<double>(), ctx->stream));
     std::vector<double> h(L.size());
@@ -468,6 +596,10 @@ int run_finish(mepi_ctx* ctx, mepi_acc* out) {
     CK(cudaMemcpyAsync(h.data(), ctx->out.p, L.size() * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaMemcpyAsync(hc, ctx->counters.p, 4 * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     ctx->d2h += L.size() * sizeof(double) + 4 * sizeof(int);
+    if (r.perk && r.count > 0) {
+        CK(cudaMemcpyAsync(out->perk, ctx->perk.p, r.count * 4 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+        ctx->d2h += r.count * 4 * sizeof(double);
+    }
     if (int r1 = stage_end(ctx, r.run_ev)) return r1;
     CK(cudaStreamSynchronize(ctx->stream));
     CK(cudaGetLastError());
@@ -504,7 +636,7 @@ int run_finish(mepi_ctx* ctx, mepi_acc* out) {
 }
 
 int run_impl(mepi_ctx* ctx, const mepi_job* job, mepi_acc* out) {
-    int rc = run_prepare(ctx, job);
+    int rc = run_prepare(ctx, job, out);
     if (!rc) rc = run_enqueue(ctx);
     if (!rc) rc = run_finish(ctx, out);
     return rc;
@@ -799,6 +931,14 @@ int mepi_set_tuning(mepi_ctx* ctx, const mepi_tuning* t) {
     return MEPI_OK;
 }
 
+int mepi_set_mem_limit(mepi_ctx* ctx, uint64_t bytes) {
+    if (!ctx) return MEPI_ERR_ARG;
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return MEPI_ERR_CUDA;
+    ctx->mem_limit = ctx->mem_budget = (size_t)bytes;
+    if (bytes && run_buffer_bytes(ctx) > bytes) release_run_buffers(ctx);
+    return MEPI_OK;
+}
+
 int mepi_get_tuning(const mepi_ctx* ctx, mepi_tuning* t) {
     if (!ctx || !t) return MEPI_ERR_ARG;
     *t = ctx->tune;
@@ -872,7 +1012,10 @@ int mepi_run_batch(int32_t n, mepi_ctx* const* ctxs, const mepi_job* jobs, mepi_
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     auto cleanup = [&](int rc) {
-        for (int i = 0; i < n; ++i) ctxs[i]->timed = true;
+        for (int i = 0; i < n; ++i) {
+            ctxs[i]->timed = true;
+            ctxs[i]->mem_budget = ctxs[i]->mem_limit;
+        }
         if (exec) cudaGraphExecDestroy(exec);
         if (graph) cudaGraphDestroy(graph);
         for (cudaEvent_t e : join)
@@ -884,10 +1027,20 @@ int mepi_run_batch(int32_t n, mepi_ctx* const* ctxs, const mepi_job* jobs, mepi_
         return rc;
     };
     try {
-        // 1. prepare every context (allocations, slabs, k lists), outside the capture
+        // 1. prepare every context (allocations, slabs, k lists), outside the capture;
+        //    the contexts share 80% of the device memory free now (their own
+        //    slabs and chunk buffers count as free: they are released first)
+        size_t free_b = 0, total_b = 0, held = 0;
+        if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return cleanup(MEPI_ERR_CUDA);
+        for (int i = 0; i < n; ++i) held += run_buffer_bytes(ctxs[i]);
+        const size_t share = (size_t)((double)(free_b + held) * 0.8 / n);
+        for (int i = 0; i < n; ++i)
+            if (run_buffer_bytes(ctxs[i]) > (ctxs[i]->mem_limit ? std::min(ctxs[i]->mem_limit, share) : share))
+                release_run_buffers(ctxs[i]);
         for (int i = 0; i < n; ++i) {
             ctxs[i]->timed = false;
-            int rc = run_prepare(ctxs[i], &jobs[i]);
+            ctxs[i]->mem_budget = ctxs[i]->mem_limit ? std::min(ctxs[i]->mem_limit, share) : share;
+            int rc = run_prepare(ctxs[i], &jobs[i], &accs[i]);
             if (rc) return cleanup(rc);
         }
         for (int i = 0; i < n; ++i)
@@ -937,7 +1090,8 @@ int mepi_destroy(mepi_ctx* ctx) {
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     for (DevBuf* b : {&ctx->S, &ctx->R, &ctx->tau, &ctx->W, &ctx->E, &ctx->E64, &ctx->H64, &ctx->U, &ctx->HA,
                       &ctx->OD, &ctx->V, &ctx->CSV,
-                      &ctx->ODH, &ctx->flags, &ctx->klist, &ctx->kpts, &ctx->partials, &ctx->out, &ctx->counters})
+                      &ctx->ODH, &ctx->flags, &ctx->klist, &ctx->kpts, &ctx->partials, &ctx->out, &ctx->counters,
+                      &ctx->jlist, &ctx->kpos, &ctx->rpos, &ctx->perk, &ctx->kcol})
         b->release();
     for (auto& ev : ctx->events) {
         cudaEventDestroy(ev.a);

@@ -39,12 +39,13 @@ __device__ __forceinline__ cplx<double> phase(double k, int R) {
     return mk(c, s);
 }
 
-// G1[qx][iy][iz][e] = sum_ix phase(kx, Rx0 + ix) box[ix][iy][iz][e],  e = blk * NN + pair
+// G1[qx][iy][iz][e] = sum_ix phase(kx, Rx0 + ix) box[ix][iy][iz][e],  e = blk * NN + pair,
+// for the qx of one slab [qx0, qx0 + gridDim.z)
 __global__ void sep_stage_a(const cplx<double>* __restrict__ box, cplx<double>* __restrict__ G1, int EL, int nbx,
-                            int nby, int nbz, int rx0, int n1) {
-    const int yz = blockIdx.y, qx = blockIdx.z;
+                            int nby, int nbz, int rx0, int n1, int qx0) {
+    const int yz = blockIdx.y, qx = blockIdx.z;   // qx relative to the slab's first qx0
     __shared__ cplx<double> ph[32];
-    if (threadIdx.x < nbx) ph[threadIdx.x] = phase(mp_coord(qx, n1), rx0 + (int)threadIdx.x);
+    if (threadIdx.x < nbx) ph[threadIdx.x] = phase(mp_coord(qx0 + qx, n1), rx0 + (int)threadIdx.x);
     __syncthreads();
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < EL; e += gridDim.x * blockDim.x) {
         cplx<double> acc = mk(0.0, 0.0);
@@ -53,8 +54,9 @@ __global__ void sep_stage_a(const cplx<double>* __restrict__ box, cplx<double>* 
     }
 }
 
-// G2[qx][qy][iz][e] = sum_iy phase(ky, Ry0 + iy) G1[qx][iy][iz][e]; the first
-// nbd blocks go to G2d (FP64), all blocks to G2f (FP32) when it is allocated.
+// G2[qx][qy][iz][e] = sum_iy phase(ky, Ry0 + iy) G1[qx][iy][iz][e] (qx within the
+// slab); the first nbd blocks go to G2d (FP64), all blocks to G2f (FP32) when
+// it is allocated.
 __global__ void sep_stage_b(const cplx<double>* __restrict__ G1, cplx<double>* __restrict__ G2d,
                             cplx<float>* __restrict__ G2f, int NN, int nbk, int nbd, int nby, int nbz, int ry0, int n1,
                             int n2) {
@@ -95,7 +97,7 @@ struct ItemHead {
 
 template <typename TG, int KI>
 __device__ void load_items(ItemHead<TG, KI>& h, const KRange& kr, int nbz, int rz0, size_t slab_elems,
-                           const double* __restrict__ tau, int N) {
+                           const double* __restrict__ tau, int N, int qx0, int nqx) {
     const int64_t i0 = (int64_t)blockIdx.x * KI;
     if (threadIdx.x == 0) h.n_items = (int)(kr.count - i0 < KI ? kr.count - i0 : KI);
     if (threadIdx.x < KI) {
@@ -104,7 +106,11 @@ __device__ void load_items(ItemHead<TG, KI>& h, const KRange& kr, int nbz, int r
         double k[3] = {0.0, 0.0, 0.0};
         if (i0 + it < kr.count) item_coords(kr, i0 + it, q, k);
         h.k[it][0] = k[0]; h.k[it][1] = k[1]; h.k[it][2] = k[2];
-        h.slab[it] = ((size_t)q[0] * kr.mp[1] + q[1]) * slab_elems;
+        // the caller keeps every item inside the resident slab [qx0, qx0 + nqx);
+        // an item outside it is clamped to the slab rather than read out of bounds
+        int rq = q[0] - qx0;
+        rq = rq < 0 ? 0 : (rq >= nqx ? nqx - 1 : rq);
+        h.slab[it] = ((size_t)rq * kr.mp[1] + q[1]) * slab_elems;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -159,12 +165,12 @@ __device__ __forceinline__ void column_sum(const ItemHead<TG, KI>& h, const cplx
 // written in the mixed form: its Jacobi reads the FP64 H(k).
 template <typename T, typename TG, int NB, int KI>
 __global__ void __launch_bounds__(128) sep_w_kernel(DevModel m, KRange kr, const cplx<TG>* __restrict__ G2, int nbz,
-                                                    int rz0, cplx<T>* __restrict__ W) {
+                                                    int rz0, int qx0, int nqx, cplx<T>* __restrict__ W) {
     extern __shared__ unsigned char smem_raw[];
     cplx<TG>* Xs = reinterpret_cast<cplx<TG>*>(smem_raw);  // [H, A_x, A_y, A_z][KI][blockDim]
     __shared__ ItemHead<TG, KI> h;
     const int NN = m.N * m.N, PT = blockDim.x, t = threadIdx.x;
-    load_items<TG, KI>(h, kr, nbz, rz0, (size_t)nbz * NB * NN, m.has_tau ? m.tau : nullptr, m.N);
+    load_items<TG, KI>(h, kr, nbz, rz0, (size_t)nbz * NB * NN, m.has_tau ? m.tau : nullptr, m.N, qx0, nqx);
     // every block is Hermitian and its consumers read the upper triangle:
     // threads walk the N (N + 1) / 2 elements n <= m
     const int u = blockIdx.y * PT + t;
@@ -237,11 +243,11 @@ __global__ void __launch_bounds__(128) sep_w_kernel(DevModel m, KRange kr, const
 // H64[i][pair] = psi * sum_iz phase(kz) G2d[qx][qy][iz][0][pair] for KI items
 template <int KI>
 __global__ void __launch_bounds__(128) sep_h64_kernel(const cplx<double>* __restrict__ G2, KRange kr, int N, int nbd,
-                                                      int nbz, int rz0, const double* __restrict__ tau,
-                                                      cplx<double>* __restrict__ H64) {
+                                                      int nbz, int rz0, const double* __restrict__ tau, int qx0,
+                                                      int nqx, cplx<double>* __restrict__ H64) {
     __shared__ ItemHead<double, KI> h;
     const int NN = N * N;
-    load_items<double, KI>(h, kr, nbz, rz0, (size_t)nbz * nbd * NN, tau, N);
+    load_items<double, KI>(h, kr, nbz, rz0, (size_t)nbz * nbd * NN, tau, N, qx0, nqx);
     // H is Hermitian and the eigensolver and refinement read its upper triangle
     const int u = blockIdx.y * blockDim.x + threadIdx.x;
     if (u >= N * (N + 1) / 2) return;
@@ -267,7 +273,7 @@ constexpr int kItemsH = 8;   // items per CTA of the FP64 H sums
 }  // namespace
 
 int sep_plan_build(SepPlan& p, const DevModel& m, const double* R_host, const cplx<double>* S_host, const int mp[3],
-                   bool fp64, cudaStream_t s) {
+                   bool fp64, size_t budget, cudaStream_t s) {
     if (p.ready && p.fp64 == fp64 && p.mp[0] == mp[0] && p.mp[1] == mp[1] && p.mp[2] == mp[2]) return 0;
     sep_plan_free(p);
     int lo[3] = {1 << 30, 1 << 30, 1 << 30}, hi[3] = {-(1 << 30), -(1 << 30), -(1 << 30)};
@@ -282,25 +288,31 @@ int sep_plan_build(SepPlan& p, const DevModel& m, const double* R_host, const cp
     if (nb[0] > 32 || nb[1] > 32 || nb[2] > 32) return 1;
     const int NN = m.N * m.N, nbk = m.nb, EL = nbk * NN;
     const size_t box = (size_t)nb[0] * nb[1] * nb[2];
-    const size_t slabs = (size_t)mp[0] * mp[1] * nb[2];
-    const size_t g2f_bytes = fp64 ? 0 : slabs * EL * sizeof(cplx<float>);
-    const size_t g1_bytes = (size_t)mp[0] * nb[1] * nb[2] * EL * sizeof(cplx<double>);
     const size_t box_bytes = box * EL * sizeof(cplx<double>);
-    size_t free_b = 0, total_b = 0;
-    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return 2;
-    // The slabs stay resident for the run; leave room for the per-chunk
-    // buffers.  The mixed form keeps FP64 slabs of every block when they fit
-    // (its FP64 reruns then take the separable sums too), else of H alone.
-    auto fits = [&](int nbd_) {
-        return slabs * nbd_ * NN * sizeof(cplx<double>) + g2f_bytes + g1_bytes + box_bytes <= free_b / 2;
-    };
-    int nbd = nbk;
-    if (!fits(nbd)) {
-        if (fp64) return 1;
-        nbd = 1;
-        if (!fits(nbd)) return 1;
+    // bytes per qx of the slab arrays
+    const size_t g1_q = (size_t)nb[1] * nb[2] * EL * sizeof(cplx<double>);
+    const size_t g2f_q = fp64 ? 0 : (size_t)mp[1] * nb[2] * EL * sizeof(cplx<float>);
+    auto g2d_q = [&](int nbd_) { return (size_t)mp[1] * nb[2] * nbd_ * NN * sizeof(cplx<double>); };
+    if (budget == 0) {
+        size_t free_b = 0, total_b = 0;
+        if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return 2;
+        budget = free_b / 2;   // the rest is left to the per-chunk buffers
     }
-    const size_t g2d_bytes = slabs * nbd * NN * sizeof(cplx<double>);
+    if (box_bytes >= budget) return 1;
+    const size_t room = budget - box_bytes;
+    // The whole mesh in one slab when it fits -- for the mixed form with FP64
+    // slabs of every block, so that its FP64 reruns take the separable sums
+    // too -- else slabs of nqx consecutive qx, built one after the other
+    // during the run (the mixed form then keeps FP64 slabs of H alone).
+    int nbd = fp64 ? nbk : 1, nqx = 0;
+    if (!fp64 && (size_t)mp[0] * (g1_q + g2f_q + g2d_q(nbk)) <= room) {
+        nbd = nbk;
+        nqx = mp[0];
+    } else {
+        const size_t per = g1_q + g2f_q + g2d_q(nbd);
+        nqx = (int)std::min<size_t>((size_t)mp[0], room / per);
+        if (nqx < 1) return 1;
+    }
     std::vector<cplx<double>> hb(box * EL, mk(0.0, 0.0));
     for (int r = 0; r < m.nR; ++r) {
         const int ix = (int)std::lrint(R_host[3 * r]) - lo[0], iy = (int)std::lrint(R_host[3 * r + 1]) - lo[1],
@@ -312,26 +324,15 @@ int sep_plan_build(SepPlan& p, const DevModel& m, const double* R_host, const cp
                 d = d + S_host[((size_t)r * NN + pr) * nbk + b];
             }
     }
-    cplx<double>* dbox = nullptr;
-    cplx<double>* G1 = nullptr;
-    auto cleanup = [&](int rc) {
-        if (dbox) cudaFree(dbox);
-        if (G1) cudaFree(G1);
-        if (rc) sep_plan_free(p);
+    auto fail = [&](int rc) {
+        sep_plan_free(p);
         return rc;
     };
-    if (cudaMalloc(&dbox, box_bytes) != cudaSuccess) return cleanup(3);
-    if (cudaMalloc(&G1, g1_bytes) != cudaSuccess) return cleanup(3);
-    if (cudaMalloc(&p.G2d, g2d_bytes) != cudaSuccess) return cleanup(3);
-    if (!fp64 && cudaMalloc(&p.G2f, g2f_bytes) != cudaSuccess) return cleanup(3);
-    if (cudaMemcpyAsync(dbox, hb.data(), box_bytes, cudaMemcpyHostToDevice, s) != cudaSuccess) return cleanup(2);
-    dim3 ga((EL + 255) / 256, nb[1] * nb[2], mp[0]);
-    sep_stage_a<<<ga, 256, 0, s>>>(dbox, G1, EL, nb[0], nb[1], nb[2], lo[0], mp[0]);
-    dim3 gb((EL + 255) / 256, mp[1] * nb[2], mp[0]);
-    sep_stage_b<<<gb, 256, 0, s>>>(G1, p.G2d, p.G2f, NN, nbk, nbd, nb[1], nb[2], lo[1], mp[0], mp[1]);
-    if (cudaGetLastError() != cudaSuccess) return cleanup(2);
-    // the temporaries are freed only after the stage kernels have run
-    if (cudaStreamSynchronize(s) != cudaSuccess) return cleanup(2);
+    if (cudaMalloc(&p.box, box_bytes) != cudaSuccess) return fail(3);
+    if (cudaMalloc(&p.G1, (size_t)nqx * g1_q) != cudaSuccess) return fail(3);
+    if (cudaMalloc(&p.G2d, (size_t)nqx * g2d_q(nbd)) != cudaSuccess) return fail(3);
+    if (!fp64 && cudaMalloc(&p.G2f, (size_t)nqx * g2f_q) != cudaSuccess) return fail(3);
+    if (cudaMemcpyAsync(p.box, hb.data(), box_bytes, cudaMemcpyHostToDevice, s) != cudaSuccess) return fail(2);
     for (int a = 0; a < 3; ++a) {
         p.mp[a] = mp[a];
         p.lo[a] = lo[a];
@@ -340,16 +341,35 @@ int sep_plan_build(SepPlan& p, const DevModel& m, const double* R_host, const cp
     p.N = m.N;
     p.nbk = nbk;
     p.nbd = nbd;
+    p.nqx = nqx;
     p.fp64 = fp64;
     p.tau = m.has_tau ? m.tau : nullptr;
     p.h2d_bytes = box_bytes;
+    p.dev_bytes = box_bytes + (size_t)nqx * (g1_q + g2f_q + g2d_q(nbd));
+    p.built_qx0 = -1;
+    if (nqx == mp[0] && launch_sep_slab(p, 0, s) != cudaSuccess) return fail(2);
+    // the host box is read by the copy above: wait for it before it goes
+    if (cudaStreamSynchronize(s) != cudaSuccess) return fail(2);
     p.ready = true;
-    return cleanup(0);
+    return 0;
+}
+
+cudaError_t launch_sep_slab(SepPlan& p, int qx0, cudaStream_t s) {
+    const int nq = std::min(p.nqx, p.mp[0] - qx0);
+    if (nq <= 0) return cudaErrorInvalidValue;
+    const int EL = p.nbk * p.N * p.N;
+    dim3 ga((EL + 255) / 256, p.nb[1] * p.nb[2], nq);
+    sep_stage_a<<<ga, 256, 0, s>>>(p.box, p.G1, EL, p.nb[0], p.nb[1], p.nb[2], p.lo[0], p.mp[0], qx0);
+    dim3 gb((EL + 255) / 256, p.mp[1] * p.nb[2], nq);
+    sep_stage_b<<<gb, 256, 0, s>>>(p.G1, p.G2d, p.G2f, p.N * p.N, p.nbk, p.nbd, p.nb[1], p.nb[2], p.lo[1], p.mp[0],
+                                   p.mp[1]);
+    p.built_qx0 = qx0;
+    return cudaGetLastError();
 }
 
 void sep_plan_free(SepPlan& p) {
-    if (p.G2d) cudaFree(p.G2d);
-    if (p.G2f) cudaFree(p.G2f);
+    for (void* q : {(void*)p.G2d, (void*)p.G2f, (void*)p.G1, (void*)p.box})
+        if (q) cudaFree(q);
     p = SepPlan();
 }
 
@@ -357,15 +377,15 @@ namespace {
 inline int pair_tile(int n_elem) { return n_elem >= 128 ? 128 : ((n_elem + 31) / 32) * 32; }
 
 template <typename T, typename TG, int NB, int KI>
-cudaError_t launch_w(const DevModel& m, const KRange& kr, const cplx<TG>* G2, int nbz, int rz0, cplx<T>* W,
-                     cudaStream_t s) {
+cudaError_t launch_w(const DevModel& m, const KRange& kr, const cplx<TG>* G2, int nbz, int rz0, int qx0, int nqx,
+                     cplx<T>* W, cudaStream_t s) {
     const int NU = m.N * (m.N + 1) / 2, PT = pair_tile(NU);
     const size_t smem = (size_t)(NB == 10 ? 4 : 1) * KI * PT * sizeof(cplx<TG>);
     cudaError_t e = cudaFuncSetAttribute(sep_w_kernel<T, TG, NB, KI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
     if (e != cudaSuccess) return e;
     dim3 grid((unsigned)((kr.count + KI - 1) / KI), (unsigned)((NU + PT - 1) / PT));
-    sep_w_kernel<T, TG, NB, KI><<<grid, PT, smem, s>>>(m, kr, G2, nbz, rz0, W);
+    sep_w_kernel<T, TG, NB, KI><<<grid, PT, smem, s>>>(m, kr, G2, nbz, rz0, qx0, nqx, W);
     return cudaGetLastError();
 }
 }  // namespace
@@ -374,7 +394,8 @@ cudaError_t launch_sep_h64(const SepPlan& p, const KRange& kr, cplx<double>* H64
     if (kr.count <= 0) return cudaSuccess;
     const int NU = p.N * (p.N + 1) / 2, PT = pair_tile(NU);
     dim3 grid((unsigned)((kr.count + kItemsH - 1) / kItemsH), (unsigned)((NU + PT - 1) / PT));
-    sep_h64_kernel<kItemsH><<<grid, PT, 0, s>>>(p.G2d, kr, p.N, p.nbd, p.nb[2], p.lo[2], p.tau, H64);
+    sep_h64_kernel<kItemsH><<<grid, PT, 0, s>>>(p.G2d, kr, p.N, p.nbd, p.nb[2], p.lo[2], p.tau, p.built_qx0, p.nqx,
+                                                H64);
     return cudaGetLastError();
 }
 
@@ -383,11 +404,11 @@ cudaError_t launch_sep_w(const SepPlan& p, const DevModel& m, const KRange& kr, 
     if (kr.count <= 0) return cudaSuccess;
     if (sizeof(T) == 8) {
         if (p.nbd != p.nbk) return cudaErrorInvalidValue;  // FP64 output needs FP64 slabs of every block
-        if (m.nb == 10) return launch_w<T, double, 10, kItemsD>(m, kr, p.G2d, p.nb[2], p.lo[2], W, s);
-        return launch_w<T, double, 4, kItemsD>(m, kr, p.G2d, p.nb[2], p.lo[2], W, s);
+        if (m.nb == 10) return launch_w<T, double, 10, kItemsD>(m, kr, p.G2d, p.nb[2], p.lo[2], p.built_qx0, p.nqx, W, s);
+        return launch_w<T, double, 4, kItemsD>(m, kr, p.G2d, p.nb[2], p.lo[2], p.built_qx0, p.nqx, W, s);
     }
-    if (m.nb == 10) return launch_w<T, float, 10, kItemsF>(m, kr, p.G2f, p.nb[2], p.lo[2], W, s);
-    return launch_w<T, float, 4, kItemsF>(m, kr, p.G2f, p.nb[2], p.lo[2], W, s);
+    if (m.nb == 10) return launch_w<T, float, 10, kItemsF>(m, kr, p.G2f, p.nb[2], p.lo[2], p.built_qx0, p.nqx, W, s);
+    return launch_w<T, float, 4, kItemsF>(m, kr, p.G2f, p.nb[2], p.lo[2], p.built_qx0, p.nqx, W, s);
 }
 
 template cudaError_t launch_sep_w<double>(const SepPlan&, const DevModel&, const KRange&, cplx<double>*, cudaStream_t);

@@ -394,27 +394,42 @@ template <typename T>
 cudaError_t launch_bandsum(const DevModel& m, const JobDev& j, int64_t nk, const double* E, const cplx<T>* V,
                            const T* CSV, const int* skip, double* partials, int n_cta, cudaStream_t s);
 cudaError_t launch_reduce(const double* partials, int n_cta, int size, double* out, cudaStream_t s);
+// per-k AHC integrand and gap at one Fermi energy into out[pos][4] (pos null: pos0 + k)
+template <typename T>
+cudaError_t launch_perk(int N, int64_t nk, const double* E, const cplx<T>* V, double ef, double T_kelvin,
+                        const int64_t* pos, int64_t pos0, double* out, cudaStream_t s);
 template <typename T>
 cudaError_t launch_opt_hall(const DevModel& m, const JobDev& j, int64_t nk, const double* E, const cplx<T>* V,
                             const int* skip, double* partials, int n_cta, cudaStream_t s);
 
-// Separable Fourier sums on a Monkhorst-Pack mesh (ft_sep.cu).  The slabs
-// G2[qx][qy][iz][blk][pair] stay resident in HBM for the run.
+// Separable Fourier sums on a Monkhorst-Pack mesh (ft_sep.cu).  The R box
+// stays resident; the slabs G2[qx][qy][iz][blk][pair] cover nqx consecutive qx
+// (the whole mesh when they fit in the memory budget, else one slab after the
+// other during the run).
 struct SepPlan {
     bool ready = false;
     bool fp64 = false;              // built for the FP64 form (no FP32 slabs)
     int N = 0, nbk = 0, nbd = 0;    // n_wf, stack blocks, blocks in G2d (nbk, or 1 = H alone)
     int mp[3] = {0, 0, 0}, lo[3] = {0, 0, 0}, nb[3] = {0, 0, 0};  // mesh, R box origin and size
+    int nqx = 0;                    // qx per slab
+    int built_qx0 = -1;             // first qx of the slab the arrays hold
+    cplx<double>* box = nullptr;    // the stack on the R box, [ix][iy][iz][blk][pair]
+    cplx<double>* G1 = nullptr;     // [qx][iy][iz][blk][pair] of one slab
     cplx<double>* G2d = nullptr;
     cplx<float>* G2f = nullptr;
     const double* tau = nullptr;
     size_t h2d_bytes = 0;
+    size_t dev_bytes = 0;           // device memory the plan holds
+    bool whole() const { return nqx == mp[0]; }
 };
 // 0: plan ready; 1: the model or mesh has no separable form here (non-integer
-// R, an R box wider than 32, or slabs larger than half the free memory);
-// 2/3: CUDA error / out of memory (the MEPI_ERR_* values).
+// R, an R box wider than 32, or not even one qx slab within the budget);
+// 2/3: CUDA error / out of memory (the MEPI_ERR_* values).  budget 0 = half the
+// free device memory.
 int sep_plan_build(SepPlan& p, const DevModel& m, const double* R_host, const cplx<double>* S_host, const int mp[3],
-                   bool fp64, cudaStream_t s);
+                   bool fp64, size_t budget, cudaStream_t s);
+// enqueue the build of the slab that starts at qx0 (stream work only)
+cudaError_t launch_sep_slab(SepPlan& p, int qx0, cudaStream_t s);
 void sep_plan_free(SepPlan& p);
 cudaError_t launch_sep_h64(const SepPlan& p, const KRange& kr, cplx<double>* H64, cudaStream_t s);
 template <typename T>

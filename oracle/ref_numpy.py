@@ -335,14 +335,28 @@ def interp_k(model: dict, kpts: np.ndarray):
     return E, U, V, A_out, Om_out
 
 
-def run(model: dict, job: dict, k_indices=None, batch: int = 64) -> dict:
+def gap_at(E: np.ndarray, ef: float) -> np.ndarray:
+    """E_c - E_v across ef per k (twice the distance to the nearest band when
+    ef lies outside all bands)."""
+    N = E.shape[1]
+    nF = (E < ef).sum(axis=1)
+    inner = np.clip(nF, 1, N - 1)
+    rows = np.arange(E.shape[0])
+    gap = E[rows, inner] - E[rows, inner - 1]
+    gap = np.where(nF == 0, 2.0 * (E[:, 0] - ef), gap)
+    return np.where(nF == N, 2.0 * (ef - E[:, -1]), gap)
+
+
+def run(model: dict, job: dict, k_indices=None, batch: int = 64, perk: bool = False) -> dict:
     """Body of the k-loop, src/core.f90:165-270, summed over the given k.
 
     Returns the unnormalised local sums (the reference's *_loc arrays):
     Ne_sum (n_eF,), ahc (3,3,n_eF), mep_ic/lc/cs (3,3,n_val),
     kubo_mep_ic/lc/cs (3,3,n_eF), n_k; with job["hw_lst"] (Hartree) and
     do_ahc also velo_ahc and kubo_ohc (3,3,n_hw,n_eF) complex, smeared by
-    i * job["eta_smr"] (src/input_paras.f90:181).
+    i * job["eta_smr"] (src/input_paras.f90:181).  With ``perk`` also
+    "perk" (n_k, 4): per k the (y,z), (z,x), (x,y) entries of its
+    kubo_ahc_tens term at ef_lst[0] and the band gap across ef_lst[0].
     """
     mp = job["mp_grid"]
     nk_tot = int(mp[0]) * int(mp[1]) * int(mp[2])
@@ -369,11 +383,16 @@ def run(model: dict, job: dict, k_indices=None, batch: int = 64) -> dict:
         eta = float(job.get("eta_smr", 0.0))
         out["velo_ahc"] = np.zeros((3, 3, hw.size, n_eF), complex)
         out["kubo_ohc"] = np.zeros((3, 3, hw.size, n_eF), complex)
+    if perk:
+        out["perk"] = np.zeros((len(k_indices), 4))
     for s in range(0, len(k_indices), batch):
         kidx = np.asarray(k_indices[s:s + batch])
         kpts = rel_kpts(mp, kidx)
         E, U, V, A, Om = interp_k(model, kpts)
         f = fd_stat(E, ef, T)                                   # (k,e,n)
+        if perk:
+            a = kubo_ahc(E, V, f[:, :1, :])[..., 0]             # (k,3,3) at ef_lst[0]
+            out["perk"][s:s + kidx.size] = np.stack([a[:, 1, 2], a[:, 2, 0], a[:, 0, 1], gap_at(E, ef[0])], axis=1)
         out["Ne_sum"] += f.sum(axis=(0, 2))                     # :187
         if do_mep:
             ic, lc, cs = mep_niu(model, E, V, A, Om, n_val)
