@@ -122,6 +122,90 @@ def random_tb_model(n_wf: int = 8, r_max: int = 1, decay: float = 1.0, seed: int
                    wf_centers=tau, a_latt=a_bohr * np.eye(3), kubo_tol=kubo_tol)
 
 
+def bloch_hamiltonian(model: TBModel, kpts: np.ndarray) -> np.ndarray:
+    """H(k) (nk, N, N) of a model in its own phase convention (numpy; used to
+    place the near-crossings of :func:`near_crossing_model`)."""
+    kpts = np.atleast_2d(np.asarray(kpts, np.float64))
+    Hk = np.einsum("kr,rnm->knm", np.exp(2j * np.pi * kpts @ model.R_frac.T), model.H)
+    if model.wf_centers is not None:
+        d = model.wf_centers[None, :, :] - model.wf_centers[:, None, :]          # tau_m - tau_n at [n, m]
+        Hk = Hk * np.exp(2j * np.pi * np.einsum("ka,nma->knm", kpts, d))
+    return Hk
+
+
+def _r0_phase(model: TBModel, k0: np.ndarray) -> np.ndarray:
+    """exp(2 pi i k0.(tau_m - tau_n)): how H(R=0) enters H(k0)."""
+    if model.wf_centers is None:
+        return np.ones((model.n_wf, model.n_wf), np.complex128)
+    d = model.wf_centers[None, :, :] - model.wf_centers[:, None, :]
+    return np.exp(2j * np.pi * d @ k0)
+
+
+def near_crossing_model(n_wf: int = 16, r_max: int = 2, decay: float = 1.5, seed: int = 4,
+                        gaps_ev=(1e-3, 2e-3, 3.5e-3, 5e-3), ef_ev: float = 0.0, n_scan: int = 20,
+                        min_sep: float = 0.2, sweeps: int = 12):
+    """A random model (:func:`random_tb_model`) with len(gaps_ev) seeded
+    near-crossings: at k-points k_j where the gap between bands N/2-1 and N/2
+    has a local minimum, that gap is lowered to gaps_ev[j] and centred on the
+    Fermi energy ef_ev.
+
+    The k_j are the deepest local minima of that gap on an n_scan^3 mesh, at
+    least ``min_sep`` apart, among those where ef_ev already lies between the
+    two bands.  At each k_j a Hermitian change of H(R=0) acts in k-space as
+    X_j = alpha (|c><c| - |v><v|) + beta (|c><c| + |v><v|) on the two band
+    states there, which moves their energies to ef -+ gap/2 and leaves the
+    other states at k_j untouched.  The changes for different k_j disturb one
+    another slightly, so they are repeated until every gap is met.
+
+    Returns (model, info) with info = {"k": (n, 3), "gap_ev": achieved gaps}.
+    """
+    model = random_tb_model(n_wf=n_wf, r_max=r_max, decay=decay, seed=seed)
+    nv = n_wf // 2
+    ef = ef_ev / AU_TO_EV
+    q = (2.0 * np.arange(1, n_scan + 1) - n_scan - 1) / (2.0 * n_scan)
+    kz, ky, kx = np.meshgrid(q, q, q, indexing="ij")
+    grid = np.stack([kx.ravel(), ky.ravel(), kz.ravel()], axis=1)
+    E = np.linalg.eigvalsh(bloch_hamiltonian(model, grid))
+    gap = (E[:, nv] - E[:, nv - 1]).reshape(n_scan, n_scan, n_scan)
+    inside = ((E[:, nv - 1] < ef) & (E[:, nv] > ef)).reshape(gap.shape)
+    is_min = inside.copy()
+    for ax in range(3):
+        for sh in (-1, 1):
+            is_min &= gap <= np.roll(gap, sh, axis=ax)
+    cand = np.argsort(np.where(is_min, gap, np.inf).ravel())
+    chosen = []
+    for c in cand:
+        if not is_min.ravel()[c]:
+            break
+        k = grid[c]
+        dk = np.array([np.abs(((k - o) + 0.5) % 1.0 - 0.5).max() for o in chosen]) if chosen else np.array([1.0])
+        if dk.min() >= min_sep:
+            chosen.append(k)
+        if len(chosen) == len(gaps_ev):
+            break
+    if len(chosen) < len(gaps_ev):
+        raise ValueError("not enough separated gap minima with ef inside the gap")
+    H0 = int(np.argmin(np.abs(model.R_frac).sum(axis=1)))
+    targets = np.asarray(gaps_ev, np.float64) / AU_TO_EV
+    for _ in range(sweeps):
+        worst = 0.0
+        for k0, g in zip(chosen, targets):
+            w, U = np.linalg.eigh(bloch_hamiltonian(model, k0)[0])
+            v, c = U[:, nv - 1], U[:, nv]
+            alpha = 0.5 * (g - (w[nv] - w[nv - 1]))
+            beta = ef - 0.5 * (w[nv] + w[nv - 1])
+            worst = max(worst, abs(w[nv] - w[nv - 1] - g), abs(0.5 * (w[nv] + w[nv - 1]) - ef))
+            X = (alpha + beta) * np.outer(c, c.conj()) + (beta - alpha) * np.outer(v, v.conj())
+            model.H[H0] += np.conj(_r0_phase(model, k0)) * X
+        if worst < 1e-9 / AU_TO_EV:
+            break
+    achieved = []
+    for k0 in chosen:
+        w = np.linalg.eigvalsh(bloch_hamiltonian(model, k0)[0])
+        achieved.append((w[nv] - w[nv - 1]) * AU_TO_EV)
+    return model, {"k": np.asarray(chosen), "gap_ev": np.asarray(achieved)}
+
+
 # Workloads: the model, mesh and Fermi settings each benchmark configuration uses.
 # Every workload runs the reference's AHE job in full: with do_ahc it also forms
 # velo_ahc_tens and kubo_ohc_tens (src/core.f90:221-230), here at one photon

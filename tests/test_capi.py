@@ -1,5 +1,5 @@
 """CPU checks of the C ABI boundary: the library builds, loads, exports every
-function include/mepi.h declares, its ctypes mirror has the header's struct
+function include/*.h declares, its ctypes mirror has mepi.h's struct
 layouts, and argument validation answers before any device work."""
 import ctypes as C
 import os
@@ -23,14 +23,15 @@ def lib():
 
 
 def header_functions():
-    txt = open(HEADER).read()
+    inc = os.path.join(ROOT, "include")
+    txt = "".join(open(os.path.join(inc, h)).read() for h in sorted(os.listdir(inc)) if h.endswith(".h"))
     return sorted(set(re.findall(r"^\s*(?:const\s+)?\w+\s*\*?\s*(mepi_\w+)\s*\(", txt, flags=re.M)))
 
 
 def test_exports_every_declared_symbol(lib):
     names = header_functions()
     assert {"mepi_create", "mepi_run", "mepi_destroy", "mepi_strerror", "mepi_interp_k", "mepi_run_batch",
-            "mepi_autotune"} <= set(names)
+            "mepi_autotune", "mepi_set_mem_limit", "mepi_mlp_create", "mepi_mlp_train"} <= set(names)
     for n in names:
         assert hasattr(lib, n), n
 
