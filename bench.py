@@ -56,6 +56,13 @@ def parse():
     p.add_argument("--chunk", type=int, default=0, help="k-points per chunk (0 = the library's default)")
     p.add_argument("--k-stride", type=int, default=1,
                    help="process every k-stride-th k-point of the mesh (small cases for profiling)")
+    p.add_argument("--form", choices=["kloop", "batched", "adaptive"], default="kloop",
+                   help="kloop: the headline k-loop (default); batched: many models in one CUDA graph launch; "
+                        "adaptive: learned-proposal refinement against uniform refinement")
+    p.add_argument("--batch-models", type=int, default=64, help="batched form: number of models")
+    p.add_argument("--no-autotune", action="store_true", help="batched form: skip the autotuner")
+    p.add_argument("--coarse", type=int, default=48, help="adaptive form: coarse mesh edge")
+    p.add_argument("--sub", type=int, default=6, help="adaptive form: sub-mesh edge per refined cell")
     p.add_argument("--fp64-check", type=int, default=-1,
                    help="k-points on which the plain FP64 path is run for the error report and its own "
                         "throughput: -1 = the whole mesh (reusing the timed mixed result), N > 0 = a strided "
@@ -394,11 +401,162 @@ def run_gpu(args, rank, world):
         print(json.dumps(out))
 
 
+def _rel_max(a, b):
+    import numpy as np
+    a, b = np.asarray(a), np.asarray(b)
+    s = float(np.abs(b).max())
+    return float(np.abs(a - b).max() / s) if s > 0 else float(np.abs(a).max())
+
+
+def run_batched(args, rank, world):
+    """Batched form: independent models of uneven size, each with a 201-energy
+    Fermi sweep, in one graph-captured launch (mepi_run_batch), against the
+    same models run one after the other."""
+    import numpy as np
+    import torch
+    from mepinterp_gb300 import api
+    from mepinterp_gb300.generator import batch_workload
+
+    work = batch_workload(args.batch_models)
+    prec = api.PREC_MIXED if args.precision == "mixed" else api.PREC_FP64
+    nk = int(sum(np.prod(j["mp_grid"]) for _, j in work))
+    t0 = time.perf_counter()
+    ctxs = [api.Context(m) for m, _ in work]
+    create_s = time.perf_counter() - t0
+    tuned, t0 = {}, time.perf_counter()
+    if not args.no_autotune:
+        for c, (m, j) in zip(ctxs, work):
+            key = (m.n_wf, m.n_R)
+            if key not in tuned:
+                tuned[key] = c.autotune(j, precision=prec, sample_k=8192)
+            else:
+                t = tuned[key]
+                c.set_tuning(t["jacobi_threads"], t["jacobi_kblock"], t["chunk_k"])
+    tune_s = time.perf_counter() - t0
+    jobs = [j for _, j in work]
+    for _ in range(max(args.warmup, 1)):
+        api.run_batch(ctxs, jobs, prec)
+    clocks = ClockSampler()
+    torch.cuda.synchronize()
+    clocks.start()
+    wall, graph = [], []
+    res = None
+    for _ in range(args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        res, gms = api.run_batch(ctxs, jobs, prec)
+        wall.append(time.perf_counter() - t0)
+        graph.append(gms)
+    clk = clocks.stop()
+    # the same models one after the other through mepi_run
+    t0 = time.perf_counter()
+    seq_dev_ms = 0.0
+    seq = []
+    for c, j in zip(ctxs, jobs):
+        seq.append(c.core_worker_loc(j, precision=prec))
+        seq_dev_ms += c.timing()["run_ms"]
+    seq_s = time.perf_counter() - t0
+    diff = max(_rel_max(a[k], b[k]) for a, b in zip(res, seq) for k in ("ahc", "mep_ic", "kubo_mep_ic"))
+    for c in ctxs:
+        c.close()
+    value = nk * args.steps / sum(wall)
+    Ns = [m.n_wf for m, _ in work]
+    out = {
+        "metric": "k-points/s, batched form", "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": max(args.warmup, 1), "ms_per_step": 1e3 * sum(wall) / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 (f64 H(k), eigen-residual, energies, k-sums)"
+        if prec == api.PREC_MIXED else "f64", "data": "synthetic (seeded random tight-binding models)",
+        "config": {"workload": f"batch{len(work)}", "models": len(work), "k_points_per_step": nk,
+                   "n_wf_range": [min(Ns), max(Ns)], "n_eF": 201, "T_kelvin": 290.1, "form": args.precision,
+                   "autotune": not args.no_autotune, "distinct_tuning_buckets": len(tuned)},
+        "graph_ms_per_step": statistics.median(graph),
+        "graph_value": nk / (statistics.median(graph) * 1e-3),
+        "sequential": {"value": nk / seq_s, "device_value": nk / (seq_dev_ms * 1e-3), "seconds": seq_s},
+        "speedup_vs_sequential": (nk / (sum(wall) / args.steps)) / (nk / seq_s),
+        "batch_vs_sequential_max_rel_diff": diff,
+        "create_s": create_s, "autotune_s": tune_s, "clocks": clk,
+    }
+    if rank == 0:
+        print(json.dumps(out))
+
+
+def run_adaptive(args, rank, world):
+    """Learned-proposal refinement of the near-crossing model against uniform
+    refinement by the plain FP64 method on the (s n)^3 mesh."""
+    import numpy as np
+    import torch
+    from mepinterp_gb300 import adaptive as AD
+    from mepinterp_gb300 import api
+    from mepinterp_gb300.generator import near_crossing_model
+
+    model, info = near_crossing_model()
+    n, s = args.coarse, args.sub
+    job = dict(mp_grid=(n, n, n), ef_lst=np.array([0.0]), T_kelvin=0.0, valence_bands=model.n_wf // 2)
+    mep = lambda r: (r["mep_ic"] + r["mep_lc"] + r["mep_cs"]).sum(axis=2)
+
+    def errs(r, ref):
+        return {"sigma_xy": float(abs(r["ahc"][0, 1, 0] - ref["ahc"][0, 1, 0]) / abs(ref["ahc"][0, 1, 0])),
+                "ahc": _rel_max(r["ahc"][:, :, 0], ref["ahc"][:, :, 0]), "mep_tensor": _rel_max(mep(r), mep(ref))}
+
+    with api.Context(model) as ctx:
+        for _ in range(max(args.warmup, 1)):
+            AD.adaptive(ctx, job, n=n, s=s)
+        clocks = ClockSampler()
+        torch.cuda.synchronize()
+        clocks.start()
+        wall, res = [], None
+        for st in range(args.steps):
+            t0 = time.perf_counter()
+            res = AD.adaptive(ctx, job, n=n, s=s, seed=st)
+            wall.append(time.perf_counter() - t0)
+        clk = clocks.stop()
+        t0 = time.perf_counter()
+        uni = AD.uniform(ctx, job, n, s, precision=api.PREC_FP64)
+        uni_s = time.perf_counter() - t0
+        uni_dev_s = ctx.timing()["run_ms"] * 1e-3
+        t0 = time.perf_counter()
+        uni_m = AD.uniform(ctx, job, n, s, precision=api.PREC_MIXED)
+        uni_m_s = time.perf_counter() - t0
+        others = {sel: errs(AD.adaptive(ctx, job, n=n, s=s, selector=sel), uni) for sel in ("none", "random", "omega")}
+        # a uniform mesh with about as many k-points as the adaptive run evaluated
+        m_eq = int(round(res["n_k_evaluated"] ** (1.0 / 3.0)))
+        t0 = time.perf_counter()
+        same = ctx.core_worker_loc(dict(job, mp_grid=(m_eq,) * 3), precision=api.PREC_MIXED)
+        same_s = time.perf_counter() - t0
+        same = {k: same[k] * (n ** 3 / m_eq ** 3) for k in AD.SUM_KEYS}
+    nf = (n * s) ** 3
+    t_ad = statistics.median(wall)
+    out = {
+        "metric": "uniform-equivalent k-points/s, adaptive form", "value": nf / t_ad, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": max(args.warmup, 1), "ms_per_step": 1e3 * t_ad, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 per-k work + bf16 proposal network",
+        "data": "synthetic (seeded random tight-binding model with 4 near-crossings)",
+        "config": {"workload": f"nearx16_r2_k{n}x{s}", "n_wf": model.n_wf, "n_R": model.n_R, "coarse": n, "sub": s,
+                   "fine_equivalent": n * s, "crossing_gaps_ev": [float(g) for g in info["gap_ev"]],
+                   "refined_fraction": res["cells_refined"] / n ** 3},
+        "k_points_evaluated": res["n_k_evaluated"],
+        "error_vs_uniform_fp64": errs(res, uni),
+        "error_of_other_selectors": others,
+        "uniform_fp64": {"seconds": uni_s, "device_seconds": uni_dev_s, "value": nf / uni_s},
+        "uniform_mixed": {"seconds": uni_m_s, "value": nf / uni_m_s, "error": errs(uni_m, uni)},
+        "uniform_same_budget": {"mesh": m_eq, "seconds": same_s, "error": errs(same, uni)},
+        "speedup_vs_uniform_fp64": uni_s / t_ad,
+        "proposal_loss": [float(res["loss_hist"][0]), float(res["loss_hist"][-1])],
+        "clocks": clk,
+    }
+    if rank == 0:
+        print(json.dumps(out))
+
+
 def main():
     args = parse()
     rank, world = dist_setup()
     if args.impl == "reference":
         run_reference(args, rank, world)
+    elif args.form == "batched":
+        run_batched(args, rank, world)
+    elif args.form == "adaptive":
+        run_adaptive(args, rank, world)
     else:
         run_gpu(args, rank, world)
     if world > 1:

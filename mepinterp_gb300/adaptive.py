@@ -9,9 +9,12 @@ this module spends the k-points where they matter instead:
    (each k-point's AHC term and the gap across E_F, mepi_acc.perk);
 2. every coarse cell gets a feature vector (see :func:`cell_features`): its k,
    log gap, and the log |Omega| of itself and its 26 neighbours;
-3. a random sample of cells is refined with the s^3 sub-mesh (the fine mesh
-   (s n)^3 restricted to the cell, run through mepi_job.k_list); the label of
-   a cell is how much refinement moves its AHC term,
+3. a sample of cells is refined with the s^3 sub-mesh (the fine mesh
+   (s n)^3 restricted to the cell, run through mepi_job.k_list): half drawn
+   uniformly from all cells, half from the 5% with the smallest coarse gaps
+   or the largest coarse |Omega| (the cells that can matter are rare, and a
+   uniform sample alone holds too few of them to learn from); the label of a
+   cell is how much refinement moves its AHC term,
    log10(eps + sum_c |mean_sub Omega_c - Omega_c(centre)|);
 4. the proposal network (include/mepi_mlp.h, trained on the GPU) is trained
    on (features, label) of the sampled cells and predicts the label of every
@@ -69,14 +72,6 @@ def cell_features(perk: np.ndarray, n: int) -> np.ndarray:
             for dx in (-1, 0, 1):
                 nb.append(np.roll(lo, (-dz, -dy, -dx), axis=(0, 1, 2)).ravel())
     return np.concatenate([kf, gap[:, None], np.stack(nb, axis=1)], axis=1).astype(np.float32)
-
-
-def _sum_dicts(a: dict, b: dict, sb: float = 1.0) -> dict:
-    out = {}
-    for key in a:
-        if key in b and isinstance(a[key], np.ndarray) and key != "perk":
-            out[key] = a[key] + sb * b[key]
-    return out
 
 
 def _job(job: dict, n: int) -> dict:
@@ -143,7 +138,12 @@ def adaptive(ctx: api.Context, job: dict, n: int = 48, s: int = 6, frac: float =
         parts = [refine_cells(ctx, job, n, s, cells, precision) + (s,)]
     elif selector == "mlp":
         feats = cell_features(perk, n)
-        sample = rng.choice(n_cells, n_smp, replace=False)
+        n_pool = max(int(0.05 * n_cells), n_smp)
+        pool = np.union1d(np.argsort(np.abs(perk[:, 3]), kind="stable")[:n_pool // 2],
+                          np.argsort(-om, kind="stable")[:n_pool // 2])
+        hot = rng.choice(pool, min(n_smp // 2, pool.size), replace=False)
+        rest = np.setdiff1d(np.arange(n_cells), hot)
+        sample = np.concatenate([hot, rng.choice(rest, n_smp - hot.size, replace=False)])
         c_s, f_s = refine_cells(ctx, job, n, s, sample, precision)
         scale = float(np.median(om)) or 1.0
         lab = np.log10(cell_labels(f_s["perk"], perk[sample], s) / scale + 1e-3).astype(np.float32)

@@ -410,8 +410,11 @@ int run_prepare(mepi_ctx* ctx, const mepi_job* job, const mepi_acc* out) {
     }
     r.perk = out && out->perk;
     r.fp64 = job->precision == MEPI_PREC_FP64;
-    int64_t chunk = job->chunk_k > 0 ? job->chunk_k
-                  : ctx->tune.chunk_k > 0 ? ctx->tune.chunk_k : default_chunk(N, ctx->nb, r.fp64, ctx->mem_budget);
+    // an explicit chunk wins; a tuned one is held to the memory budget
+    const int64_t dchunk = default_chunk(N, ctx->nb, r.fp64, ctx->mem_budget);
+    int64_t chunk = job->chunk_k > 0       ? job->chunk_k
+                    : ctx->tune.chunk_k > 0 ? std::min(ctx->tune.chunk_k, ctx->mem_budget ? dchunk : ctx->tune.chunk_k)
+                                            : dchunk;
     r.chunk = std::max<int64_t>(1, std::min<int64_t>(chunk, std::max<int64_t>(r.count, 1)));
     r.degen_gap = job->degen_gap >= 0 ? job->degen_gap : 3e-3;
     r.n_hw = opt_hall ? job->n_hw : 0;
@@ -640,6 +643,35 @@ int run_impl(mepi_ctx* ctx, const mepi_job* job, mepi_acc* out) {
     if (!rc) rc = run_enqueue(ctx);
     if (!rc) rc = run_finish(ctx, out);
     return rc;
+}
+
+// Device-memory budgets of a batch: each context wants its whole-mesh slabs
+// plus its default chunk buffers (x2: the budget is split in halves); the
+// total is shared by water-filling, so small models get all they want and the
+// large ones split the rest (their slabs are then built per qx range).
+std::vector<size_t> batch_budgets(int n, mepi_ctx* const* ctxs, const mepi_job* jobs, double total) {
+    std::vector<double> want(n);
+    for (int i = 0; i < n; ++i) {
+        const bool fp64 = jobs[i].precision == MEPI_PREC_FP64;
+        const mepi_ctx* c = ctxs[i];
+        const size_t chunk = (size_t)default_chunk(c->N, c->nb, fp64) *
+                             (fp64 ? per_k_bytes<double>(c->N, c->nb) : per_k_bytes<float>(c->N, c->nb));
+        want[i] = 2.0 * (double)std::max(sep_plan_want(c->dm, c->R_host.data(), jobs[i].mp_grid, fp64), chunk);
+        if (c->mem_limit) want[i] = std::min(want[i], (double)c->mem_limit);
+    }
+    std::vector<int> ord(n);
+    for (int i = 0; i < n; ++i) ord[i] = i;
+    std::sort(ord.begin(), ord.end(), [&](int a, int b) { return want[a] < want[b]; });
+    std::vector<size_t> out(n);
+    double left = total;
+    for (int j = 0; j < n; ++j) {
+        const int i = ord[j];
+        const double fair = left / (n - j);
+        const double b = std::min(want[i], fair);
+        out[i] = (size_t)b;
+        left -= b;
+    }
+    return out;
 }
 
 // Process-wide record of tuned launch shapes, keyed by (device, N, nR, blocks).
@@ -965,10 +997,13 @@ int mepi_autotune(mepi_ctx* ctx, const mepi_job* job, int64_t sample_k, mepi_tun
         const int np = ctx->N <= 8 ? 8 : ctx->N <= 16 ? 16 : ctx->N <= 32 ? 32 : 64;
         mepi_tuning win{};
         double best_ms = 1e300;
+        // chunk candidates: the default (8 GB of per-k buffers, at most 65,536 k) and a quarter of it
+        const int64_t c_def = default_chunk(ctx->N, ctx->nb, j.precision == MEPI_PREC_FP64, ctx->mem_limit);
+        const int64_t c_q = std::max<int64_t>(64, (c_def / 4) & ~(int64_t)63);
         for (int threads : {64, 128, 256}) {
             if (threads < np / 2) continue;
             for (int kb : {4, 8, 16})
-                for (int64_t ch : {(int64_t)16384, (int64_t)65536}) {
+                for (int64_t ch : {c_q, c_def}) {
                     ctx->tune = mepi_tuning{threads, kb, ch, 0.0};
                     rc = run_impl(ctx, &j, &acc);
                     if (rc) {
@@ -1033,13 +1068,12 @@ int mepi_run_batch(int32_t n, mepi_ctx* const* ctxs, const mepi_job* jobs, mepi_
         size_t free_b = 0, total_b = 0, held = 0;
         if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return cleanup(MEPI_ERR_CUDA);
         for (int i = 0; i < n; ++i) held += run_buffer_bytes(ctxs[i]);
-        const size_t share = (size_t)((double)(free_b + held) * 0.8 / n);
+        const std::vector<size_t> budget = batch_budgets(n, ctxs, jobs, (double)(free_b + held) * 0.8);
         for (int i = 0; i < n; ++i)
-            if (run_buffer_bytes(ctxs[i]) > (ctxs[i]->mem_limit ? std::min(ctxs[i]->mem_limit, share) : share))
-                release_run_buffers(ctxs[i]);
+            if (run_buffer_bytes(ctxs[i]) > budget[i]) release_run_buffers(ctxs[i]);
         for (int i = 0; i < n; ++i) {
             ctxs[i]->timed = false;
-            ctxs[i]->mem_budget = ctxs[i]->mem_limit ? std::min(ctxs[i]->mem_limit, share) : share;
+            ctxs[i]->mem_budget = budget[i];
             int rc = run_prepare(ctxs[i], &jobs[i], &accs[i]);
             if (rc) return cleanup(rc);
         }

@@ -272,20 +272,40 @@ constexpr int kItemsH = 8;   // items per CTA of the FP64 H sums
 
 }  // namespace
 
+namespace {
+// the integer R box of the model; false when R is not integer or the box is wider than 32
+bool sep_box(const DevModel& m, const double* R_host, int lo[3], int nb[3]) {
+    int hi[3] = {-(1 << 30), -(1 << 30), -(1 << 30)};
+    lo[0] = lo[1] = lo[2] = 1 << 30;
+    for (int r = 0; r < m.nR; ++r)
+        for (int a = 0; a < 3; ++a) {
+            const double v = R_host[3 * r + a];
+            if (std::fabs(v - std::rint(v)) > 1e-9 || std::fabs(v) > 1e6) return false;
+            lo[a] = std::min(lo[a], (int)std::lrint(v));
+            hi[a] = std::max(hi[a], (int)std::lrint(v));
+        }
+    for (int a = 0; a < 3; ++a) nb[a] = hi[a] - lo[a] + 1;
+    return nb[0] <= 32 && nb[1] <= 32 && nb[2] <= 32;
+}
+}  // namespace
+
+size_t sep_plan_want(const DevModel& m, const double* R_host, const int mp[3], bool fp64) {
+    int lo[3], nb[3];
+    if (!sep_box(m, R_host, lo, nb)) return 0;
+    const size_t EL = (size_t)m.nb * m.N * m.N, NN = (size_t)m.N * m.N;
+    const size_t box = (size_t)nb[0] * nb[1] * nb[2] * EL * sizeof(cplx<double>);
+    const size_t g1 = (size_t)nb[1] * nb[2] * EL * sizeof(cplx<double>);
+    const size_t g2f = fp64 ? 0 : (size_t)mp[1] * nb[2] * EL * sizeof(cplx<float>);
+    const size_t g2d = (size_t)mp[1] * nb[2] * m.nb * NN * sizeof(cplx<double>);
+    return box + (size_t)mp[0] * (g1 + g2f + g2d);
+}
+
 int sep_plan_build(SepPlan& p, const DevModel& m, const double* R_host, const cplx<double>* S_host, const int mp[3],
                    bool fp64, size_t budget, cudaStream_t s) {
     if (p.ready && p.fp64 == fp64 && p.mp[0] == mp[0] && p.mp[1] == mp[1] && p.mp[2] == mp[2]) return 0;
     sep_plan_free(p);
-    int lo[3] = {1 << 30, 1 << 30, 1 << 30}, hi[3] = {-(1 << 30), -(1 << 30), -(1 << 30)};
-    for (int r = 0; r < m.nR; ++r)
-        for (int a = 0; a < 3; ++a) {
-            const double v = R_host[3 * r + a];
-            if (std::fabs(v - std::rint(v)) > 1e-9 || std::fabs(v) > 1e6) return 1;
-            lo[a] = std::min(lo[a], (int)std::lrint(v));
-            hi[a] = std::max(hi[a], (int)std::lrint(v));
-        }
-    const int nb[3] = {hi[0] - lo[0] + 1, hi[1] - lo[1] + 1, hi[2] - lo[2] + 1};
-    if (nb[0] > 32 || nb[1] > 32 || nb[2] > 32) return 1;
+    int lo[3], nb[3];
+    if (!sep_box(m, R_host, lo, nb)) return 1;
     const int NN = m.N * m.N, nbk = m.nb, EL = nbk * NN;
     const size_t box = (size_t)nb[0] * nb[1] * nb[2];
     const size_t box_bytes = box * EL * sizeof(cplx<double>);

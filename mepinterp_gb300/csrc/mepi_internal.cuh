@@ -428,6 +428,8 @@ struct SepPlan {
 // free device memory.
 int sep_plan_build(SepPlan& p, const DevModel& m, const double* R_host, const cplx<double>* S_host, const int mp[3],
                    bool fp64, size_t budget, cudaStream_t s);
+// device bytes of the whole-mesh plan (0: no separable form for this model)
+size_t sep_plan_want(const DevModel& m, const double* R_host, const int mp[3], bool fp64);
 // enqueue the build of the slab that starts at qx0 (stream work only)
 cudaError_t launch_sep_slab(SepPlan& p, int qx0, cudaStream_t s);
 void sep_plan_free(SepPlan& p);

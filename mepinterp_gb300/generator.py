@@ -206,6 +206,25 @@ def near_crossing_model(n_wf: int = 16, r_max: int = 2, decay: float = 1.5, seed
     return model, {"k": np.asarray(chosen), "gap_ev": np.asarray(achieved)}
 
 
+def batch_workload(n_models: int = 64, seed: int = 3):
+    """The batched form's workload: n_models independent seeded models, each
+    with nWf drawn from {4, 6, ..., 64}, an R shell radius from {1, 2, 3}
+    (nR 27-343), a mesh edge from {32, 48, 64, 96}, and a sweep of 201 Fermi
+    energies over [-1, 1] eV with 25 meV Fermi-Dirac smearing (T = 290.1 K).
+    Returns a list of (TBModel, job dict)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    ef = np.linspace(-1.0, 1.0, 201) / AU_TO_EV
+    for i in range(n_models):
+        n_wf = 2 * int(rng.integers(2, 33))
+        r_max = int(rng.integers(1, 4))
+        edge = int(rng.choice([32, 48, 64, 96]))
+        m = random_tb_model(n_wf=n_wf, r_max=r_max, decay=1.5, seed=1000 + i)
+        job = dict(mp_grid=(edge, edge, edge), ef_lst=ef, T_kelvin=290.1, valence_bands=n_wf // 2)
+        out.append((m, job))
+    return out
+
+
 # Workloads: the model, mesh and Fermi settings each benchmark configuration uses.
 # Every workload runs the reference's AHE job in full: with do_ahc it also forms
 # velo_ahc_tens and kubo_ohc_tens (src/core.f90:221-230), here at one photon
