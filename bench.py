@@ -452,9 +452,12 @@ def run_batched(args, rank, world):
     t0 = time.perf_counter()
     seq_dev_ms = 0.0
     seq = []
+    for c in ctxs:
+        c.trim()                      # the batch's buffers; each sequential run allocates its own
     for c, j in zip(ctxs, jobs):
         seq.append(c.core_worker_loc(j, precision=prec))
         seq_dev_ms += c.timing()["run_ms"]
+        c.trim()
     seq_s = time.perf_counter() - t0
     diff = max(_rel_max(a[k], b[k]) for a, b in zip(res, seq) for k in ("ahc", "mep_ic", "kubo_mep_ic"))
     for c in ctxs:

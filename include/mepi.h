@@ -202,6 +202,10 @@ int mepi_get_tuning(const mepi_ctx *ctx, mepi_tuning *t);
  * mesh are built for one range of qx after the other during the run.
  * Results do not depend on the limit. */
 int mepi_set_mem_limit(mepi_ctx *ctx, uint64_t bytes);
+/* Free the context's cached run buffers (separable slabs, chunk buffers);
+ * the next run rebuilds them.  For callers that keep many contexts and run
+ * them in turn.  No counterpart in the reference. */
+int mepi_trim(mepi_ctx *ctx);
 
 /* Batched form.  No counterpart in the reference, where each model is a
  * separate run.  n (context, job) pairs -- models of different band and R

@@ -102,6 +102,8 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
     lib.mepi_set_tuning.restype = C.c_int
     lib.mepi_set_mem_limit.argtypes = [P, C.c_uint64]
     lib.mepi_set_mem_limit.restype = C.c_int
+    lib.mepi_trim.argtypes = [P]
+    lib.mepi_trim.restype = C.c_int
     lib.mepi_get_tuning.argtypes = [P, C.POINTER(MepiTuning)]
     lib.mepi_get_tuning.restype = C.c_int
     lib.mepi_run_batch.argtypes = [C.c_int32, C.POINTER(P), C.POINTER(MepiJob), C.POINTER(MepiAcc),
@@ -230,6 +232,10 @@ class Context:
         the defaults); a large mesh under a small limit builds its slabs one
         qx range at a time.  Results do not depend on it."""
         _check(self.lib.mepi_set_mem_limit(self._h, int(nbytes)))
+
+    def trim(self) -> None:
+        """mepi_trim: free the cached slabs and chunk buffers (rebuilt on the next run)."""
+        _check(self.lib.mepi_trim(self._h))
 
     def get_wann_interp(self, kpts, precision: int = PREC_FP64):
         """en_k (nk,N), V (nk,3,N,N), A_diag (nk,3,N), Om_diag (nk,3,3,N) in C order."""

@@ -410,8 +410,20 @@ int run_prepare(mepi_ctx* ctx, const mepi_job* job, const mepi_acc* out) {
     }
     r.perk = out && out->perk;
     r.fp64 = job->precision == MEPI_PREC_FP64;
-    // an explicit chunk wins; a tuned one is held to the memory budget
-    const int64_t dchunk = default_chunk(N, ctx->nb, r.fp64, ctx->mem_budget);
+    // an explicit chunk wins; a tuned one is held to the memory budget.  Without a
+    // budget the chunk buffers take at most 40% of the memory free now (buffers
+    // this context already holds count as free: they are replaced).
+    size_t cbudget = ctx->mem_budget;
+    if (!cbudget) {
+        size_t free_b = 0, total_b = 0;
+        CK(cudaMemGetInfo(&free_b, &total_b));
+        size_t held = 0;
+        for (const DevBuf* d : {&ctx->W, &ctx->E, &ctx->E64, &ctx->H64, &ctx->U, &ctx->HA, &ctx->OD, &ctx->V,
+                                &ctx->CSV, &ctx->flags})
+            held += d->bytes;
+        cbudget = (size_t)(0.8 * (double)(free_b + held));   // halved inside default_chunk
+    }
+    const int64_t dchunk = default_chunk(N, ctx->nb, r.fp64, cbudget);
     int64_t chunk = job->chunk_k > 0       ? job->chunk_k
                     : ctx->tune.chunk_k > 0 ? std::min(ctx->tune.chunk_k, ctx->mem_budget ? dchunk : ctx->tune.chunk_k)
                                             : dchunk;
@@ -971,6 +983,13 @@ int mepi_set_mem_limit(mepi_ctx* ctx, uint64_t bytes) {
     return MEPI_OK;
 }
 
+int mepi_trim(mepi_ctx* ctx) {
+    if (!ctx) return MEPI_ERR_ARG;
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return MEPI_ERR_CUDA;
+    release_run_buffers(ctx);
+    return MEPI_OK;
+}
+
 int mepi_get_tuning(const mepi_ctx* ctx, mepi_tuning* t) {
     if (!ctx || !t) return MEPI_ERR_ARG;
     *t = ctx->tune;
@@ -1024,6 +1043,8 @@ int mepi_autotune(mepi_ctx* ctx, const mepi_job* job, int64_t sample_k, mepi_tun
             g_tune[tune_key(ctx)] = win;
         }
         if (best) *best = win;
+        // leave no run buffers behind, so that many contexts can be tuned in turn
+        release_run_buffers(ctx);
         return MEPI_OK;
     } catch (const std::bad_alloc&) {
         return MEPI_ERR_NOMEM;

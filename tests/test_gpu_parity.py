@@ -135,6 +135,8 @@ def test_odd_and_large_n(gpu_lib, n_wf):
     ref = O.run(m.as_dict(), job, batch=9)
     got = api.run(m, job, precision=api.PREC_FP64)
     check_sums(got, ref, SUM_TOL)
+    mixed = api.run(m, job, precision=api.PREC_MIXED)
+    check_sums(mixed, ref, MIXED_TOL)
 
 
 def test_femn_golden_gpu(gpu_lib):
