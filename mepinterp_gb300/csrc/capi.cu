@@ -90,6 +90,7 @@ struct mepi_ctx {
     DevBuf kcol;
     std::vector<int64_t> kcol_host;
     std::vector<int64_t> kslab;         // kcol_host index where each qx slab starts (+ the end)
+    int kslab_nqx = 0;                  // the slab width kslab was made for
     int64_t kcol_key[6] = {-1, -1, -1, -1, -1, -1};
     // launch shapes picked by mepi_autotune (0 = the built-in choice)
     mepi_tuning tune{};
@@ -304,6 +305,16 @@ int64_t default_chunk(int N, int nb, bool fp64, size_t mem_budget = 0) {
     return c;
 }
 
+// out[j] = first index of a qx-outermost k list whose qx >= j * nqx (j = 0 ..
+// n_slabs), out[n_slabs] = count
+void slab_ranges(const int64_t* L, int64_t count, int mp0, int nqx, std::vector<int64_t>& out) {
+    const int nslab = (mp0 + nqx - 1) / nqx;
+    out.assign(nslab + 1, count);
+    int j = 0;
+    for (int64_t i = 0; i < count && j < nslab; ++i)
+        while (j < nslab && (int)(L[i] % mp0) >= j * nqx) out[j++] = i;
+}
+
 // Separable sums for this run when the model, mesh and memory allow them:
 // builds (or reuses) the slabs and the (qx, qy)-column ordered k list.
 int prepare_sep(mepi_ctx* ctx, const mepi_job* job, int64_t count, bool fp64) {
@@ -370,12 +381,9 @@ int prepare_sep(mepi_ctx* ctx, const mepi_job* job, int64_t count, bool fp64) {
         ctx->kslab.clear();
     }
     // the list runs qx-outermost: each slab of nqx consecutive qx is one range of it
-    const int nslab = (mp[0] + ctx->sep.nqx - 1) / ctx->sep.nqx;
-    if ((int)ctx->kslab.size() != nslab + 1) {
-        ctx->kslab.assign(nslab + 1, count);
-        int j = 0;
-        for (int64_t i = 0; i < count && j < nslab; ++i)
-            while (j < nslab && (int)(ctx->kcol_host[i] % mp[0]) >= j * ctx->sep.nqx) ctx->kslab[j++] = i;
+    if ((int)ctx->kslab.size() < 2 || ctx->kslab_nqx != ctx->sep.nqx) {
+        slab_ranges(ctx->kcol_host.data(), count, mp[0], ctx->sep.nqx, ctx->kslab);
+        ctx->kslab_nqx = ctx->sep.nqx;
     }
     ctx->sep_active = true;
     return 0;
@@ -578,9 +586,25 @@ int run_finish(mepi_ctx* ctx, mepi_acc* out) {
                                                : job.k_begin + i * job.k_stride);
                 redo_pos.push_back(ctx->sep_active ? ctx->kpos_host[i] : i);
             }
-        // a slabbed plan holds only its last slab: the reruns take the direct sums
+        // A slabbed mixed plan holds FP32 slabs of one qx range: the reruns get
+        // FP64 slabs of every block instead, built over their own qx ranges
+        // (the reruns are in column order, qx-outermost); the next run rebuilds
+        // its plan.  Where no FP64 slab fits, the reruns take the direct sums.
         const bool sep_keep = ctx->sep_active;
-        if (!ctx->sep.whole()) ctx->sep_active = false;
+        std::vector<int64_t> rslab;
+        if (!redo.empty() && ctx->sep_active && !ctx->sep.whole()) {
+            const int mp[3] = {job.mp_grid[0], job.mp_grid[1], job.mp_grid[2]};
+            sep_plan_free(ctx->sep);
+            const int prc = sep_plan_build(ctx->sep, ctx->dm, ctx->R_host.data(), ctx->S_host.data(), mp, true,
+                                           ctx->mem_budget / 2, ctx->stream);
+            if (prc > 1) {
+                cudaGetLastError();
+                return prc;
+            }
+            if (prc == 0) ctx->h2d += ctx->sep.h2d_bytes;
+            if (prc == 0 && !ctx->sep.whole()) slab_ranges(redo.data(), (int64_t)redo.size(), mp[0], ctx->sep.nqx, rslab);
+        }
+        if (!ctx->sep.ready || (!ctx->sep.whole() && rslab.empty())) ctx->sep_active = false;
         if (!redo.empty()) {
             int64_t rchunk =
                 std::min<int64_t>(default_chunk(ctx->N, ctx->nb, true, ctx->mem_budget), (int64_t)redo.size());
@@ -595,12 +619,19 @@ int run_finish(mepi_ctx* ctx, mepi_acc* out) {
                 CK(cudaMemcpyAsync(ctx->rpos.p, redo_pos.data(), redo_pos.size() * sizeof(int64_t),
                                    cudaMemcpyHostToDevice, ctx->stream));
             }
-            for (int64_t c0 = 0; c0 < (int64_t)redo.size(); c0 += rchunk) {
-                KRange kr{0, 1, std::min<int64_t>(rchunk, (int64_t)redo.size() - c0), ctx->klist.as<int64_t>() + c0,
-                          nullptr, {job.mp_grid[0], job.mp_grid[1], job.mp_grid[2]}};
-                rc = run_chunk<double>(ctx, kr, &r.jb, r.n_cta, 0.0, false, true, nullptr);
-                if (!rc && r.perk) rc = enqueue_perk<double>(ctx, kr.count, ctx->rpos.as<int64_t>() + c0, 0);
-                if (rc) return rc;
+            if (rslab.empty()) rslab = {0, (int64_t)redo.size()};
+            for (size_t j = 0; j + 1 < rslab.size(); ++j) {
+                const int64_t b = rslab[j], e = rslab[j + 1];
+                if (e <= b) continue;
+                if (ctx->sep_active && !ctx->sep.whole())
+                    STAGE(ST_FT, launch_sep_slab(ctx->sep, (int)j * ctx->sep.nqx, ctx->stream));
+                for (int64_t c0 = b; c0 < e; c0 += rchunk) {
+                    KRange kr{0, 1, std::min<int64_t>(rchunk, e - c0), ctx->klist.as<int64_t>() + c0, nullptr,
+                              {job.mp_grid[0], job.mp_grid[1], job.mp_grid[2]}};
+                    rc = run_chunk<double>(ctx, kr, &r.jb, r.n_cta, 0.0, false, true, nullptr);
+                    if (!rc && r.perk) rc = enqueue_perk<double>(ctx, kr.count, ctx->rpos.as<int64_t>() + c0, 0);
+                    if (rc) return rc;
+                }
             }
         }
         ctx->sep_active = sep_keep;

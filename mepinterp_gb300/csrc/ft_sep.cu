@@ -16,9 +16,9 @@
 //
 // Precision: the plan is built in FP64.  The FP64 form keeps G2 in FP64 for all
 // blocks.  The mixed form keeps all blocks in FP32 (nbz-term sums of FP32
-// values, about 1e-7 relative) for its per-k work, plus FP64 slabs for the FP64
-// H(k) of the eigenpair refinement and for its FP64 reruns (all blocks when
-// they fit in memory, else H alone).
+// values, about 1e-7 relative) for its per-k work, plus FP64 slabs for the
+// FP64-accurate H(k) of the eigenpair refinement (summed in double-FP32) and
+// for its FP64 reruns (all blocks when they fit in memory, else H alone).
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -240,29 +240,111 @@ __global__ void __launch_bounds__(128) sep_w_kernel(DevModel m, KRange kr, const
     }
 }
 
-// H64[i][pair] = psi * sum_iz phase(kz) G2d[qx][qy][iz][0][pair] for KI items
+// H64[i][pair] = psi * sum_iz phase(kz) G2d[qx][qy][iz][0][pair] for KI items,
+// the FP64 H(k) of the mixed form, in double-FP32: the FP64 slab values and
+// phases are split into FP32 hi + lo parts, each product a b of two such
+// pairs is formed as p + e (p = ah bh, e = fma(ah, bh, -p) + ah bl + al bh),
+// and the nbz-term sums run in TwoSum -- about 2^-44 relative, far below what
+// the eigenpair refinement needs from H(k), with no FP64 arithmetic per term.
+struct DFc {
+    DF re, im;
+};
+__device__ __forceinline__ void split_d(double x, float& h, float& l) {
+    h = __double2float_rn(x);
+    l = __double2float_rn(x - (double)h);
+}
+// acc += (ah + al)(bh + bl)
+__device__ __forceinline__ void df_mac(DF& acc, float ah, float al, float bh, float bl) {
+    const float p = __fmul_rn(ah, bh);
+    float e = __fmaf_rn(ah, bh, -p);
+    e = __fmaf_rn(ah, bl, e);
+    e = __fmaf_rn(al, bh, e);
+    df_add(acc, p);
+    acc.c = __fadd_rn(acc.c, e);
+}
+// acc += a b for complex a = (ar, ai) hi/lo and b likewise
+__device__ __forceinline__ void dfc_mac(DFc& acc, const cplx<float>& ah, const cplx<float>& al, const cplx<float>& bh,
+                                        const cplx<float>& bl) {
+    df_mac(acc.re, ah.re, al.re, bh.re, bl.re);
+    df_mac(acc.re, -ah.im, -al.im, bh.im, bl.im);
+    df_mac(acc.im, ah.re, al.re, bh.im, bl.im);
+    df_mac(acc.im, ah.im, al.im, bh.re, bl.re);
+}
+__device__ __forceinline__ void dfc_split(const DFc& v, cplx<float>& h, cplx<float>& l) {
+    // renormalise each part so that hi carries the leading bits
+    const float rh = __fadd_rn(v.re.s, v.re.c), ih = __fadd_rn(v.im.s, v.im.c);
+    h = mk(rh, ih);
+    l = mk(__fadd_rn(__fsub_rn(v.re.s, rh), v.re.c), __fadd_rn(__fsub_rn(v.im.s, ih), v.im.c));
+}
+
 template <int KI>
-__global__ void __launch_bounds__(128) sep_h64_kernel(const cplx<double>* __restrict__ G2, KRange kr, int N, int nbd,
-                                                      int nbz, int rz0, const double* __restrict__ tau, int qx0,
-                                                      int nqx, cplx<double>* __restrict__ H64) {
+__global__ void __launch_bounds__(128) sep_h64_df_kernel(const cplx<double>* __restrict__ G2, KRange kr, int N,
+                                                         int nbd, int nbz, int rz0, const double* __restrict__ tau,
+                                                         int qx0, int nqx, cplx<double>* __restrict__ H64) {
     __shared__ ItemHead<double, KI> h;
+    __shared__ cplx<float> phh[KI][32], phl[KI][32], fih[KI][kMaxN], fil[KI][kMaxN];
     const int NN = N * N;
     load_items<double, KI>(h, kr, nbz, rz0, (size_t)nbz * nbd * NN, tau, N, qx0, nqx);
-    // H is Hermitian and the eigensolver and refinement read its upper triangle
+    for (int e = threadIdx.x; e < KI * 32; e += blockDim.x) {
+        const int it = e / 32, iz = e % 32;
+        split_d(h.ph[it][iz].re, phh[it][iz].re, phl[it][iz].re);
+        split_d(h.ph[it][iz].im, phh[it][iz].im, phl[it][iz].im);
+    }
+    if (tau)
+        for (int e = threadIdx.x; e < KI * N; e += blockDim.x) {
+            const int it = e / N, n = e % N;
+            split_d(h.phi[it][n].re, fih[it][n].re, fil[it][n].re);
+            split_d(h.phi[it][n].im, fih[it][n].im, fil[it][n].im);
+        }
+    __syncthreads();
     const int u = blockIdx.y * blockDim.x + threadIdx.x;
     if (u >= N * (N + 1) / 2) return;
     int n, mm;
     upper_pair(u, N, n, mm);
     const int pair = n * N + mm;
-    cplx<double> acc[KI];
-    column_sum<double, KI>(h, G2 + pair, (size_t)nbd * NN, nbz, acc);
+    const size_t zs = (size_t)nbd * NN;
+    DFc acc[KI];
+#pragma unroll
+    for (int it = 0; it < KI; ++it) acc[it] = DFc{DF{0.f, 0.f}, DF{0.f, 0.f}};
+    if (h.uniform) {
+        const cplx<double>* gp = G2 + pair + h.slab[0];
+        for (int iz = 0; iz < nbz; ++iz) {
+            const cplx<double> v = gp[(size_t)iz * zs];
+            cplx<float> vh, vl;
+            split_d(v.re, vh.re, vl.re);
+            split_d(v.im, vh.im, vl.im);
+#pragma unroll
+            for (int it = 0; it < KI; ++it) dfc_mac(acc[it], phh[it][iz], phl[it][iz], vh, vl);
+        }
+    } else {
+#pragma unroll
+        for (int it = 0; it < KI; ++it)
+            if (it < h.n_items)
+                for (int iz = 0; iz < nbz; ++iz) {
+                    const cplx<double> v = G2[pair + h.slab[it] + (size_t)iz * zs];
+                    cplx<float> vh, vl;
+                    split_d(v.re, vh.re, vl.re);
+                    split_d(v.im, vh.im, vl.im);
+                    dfc_mac(acc[it], phh[it][iz], phl[it][iz], vh, vl);
+                }
+    }
     const int64_t i0 = (int64_t)blockIdx.x * KI;
 #pragma unroll
     for (int it = 0; it < KI; ++it) {
         if (it >= h.n_items) break;
-        cplx<double> v = acc[it];
-        if (tau) v = cj_mul(h.phi[it][n], h.phi[it][mm]) * v;
-        H64[(size_t)(i0 + it) * NN + pair] = v;
+        DFc r = acc[it];
+        if (tau) {
+            // psi = conj(phi_n) phi_m, then psi * X
+            const cplx<float> an_h = conjg(fih[it][n]), an_l = conjg(fil[it][n]);
+            DFc ps{DF{0.f, 0.f}, DF{0.f, 0.f}};
+            dfc_mac(ps, an_h, an_l, fih[it][mm], fil[it][mm]);
+            cplx<float> psh, psl, xh, xl;
+            dfc_split(ps, psh, psl);
+            dfc_split(r, xh, xl);
+            r = DFc{DF{0.f, 0.f}, DF{0.f, 0.f}};
+            dfc_mac(r, psh, psl, xh, xl);
+        }
+        H64[(size_t)(i0 + it) * NN + pair] = mk((double)r.re.s + (double)r.re.c, (double)r.im.s + (double)r.im.c);
     }
 }
 
@@ -414,8 +496,8 @@ cudaError_t launch_sep_h64(const SepPlan& p, const KRange& kr, cplx<double>* H64
     if (kr.count <= 0) return cudaSuccess;
     const int NU = p.N * (p.N + 1) / 2, PT = pair_tile(NU);
     dim3 grid((unsigned)((kr.count + kItemsH - 1) / kItemsH), (unsigned)((NU + PT - 1) / PT));
-    sep_h64_kernel<kItemsH><<<grid, PT, 0, s>>>(p.G2d, kr, p.N, p.nbd, p.nb[2], p.lo[2], p.tau, p.built_qx0, p.nqx,
-                                                H64);
+    sep_h64_df_kernel<kItemsH><<<grid, PT, 0, s>>>(p.G2d, kr, p.N, p.nbd, p.nb[2], p.lo[2], p.tau, p.built_qx0,
+                                                   p.nqx, H64);
     return cudaGetLastError();
 }
 
