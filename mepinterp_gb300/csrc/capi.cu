@@ -105,7 +105,10 @@ struct mepi_ctx {
         JobDev jb{};
         size_t run_ev = 0;
         bool perk = false;              // per-k output requested
+        int64_t n_redo = 0;             // k-points rerun in FP64
     } run;
+    double* h_out = nullptr;            // pinned copy-back of the reduced sums and counters
+    size_t h_out_cap = 0;
     bool timed = true;                  // per-stage CUDA events (off inside a graph capture)
     size_t mem_budget = 0;              // device bytes for slabs + chunk buffers (0: the defaults)
     size_t mem_limit = 0;               // the caller's limit (mepi_set_mem_limit)
@@ -569,9 +572,11 @@ int enqueue_range(mepi_ctx* ctx, int64_t b, int64_t e) {
     return 0;
 }
 
-// Phase 3: the FP64 reruns of the mixed form, the fixed-order reduction and
-// the copy back.
-int run_finish(mepi_ctx* ctx, mepi_acc* out) {
+// Phase 3a: the FP64 reruns of the mixed form, the fixed-order reduction and
+// the asynchronous copy back into pinned memory.  The batched form enqueues
+// this for every context before collecting any, so the contexts' reruns
+// overlap on the GPU.
+int finish_enqueue(mepi_ctx* ctx) {
     mepi_ctx::Run& r = ctx->run;
     const mepi_job& job = r.job;
     const AccLayout& L = r.L;
@@ -636,18 +641,37 @@ int run_finish(mepi_ctx* ctx, mepi_acc* out) {
         }
         ctx->sep_active = sep_keep;
     }
+    r.n_redo = (int64_t)redo.size();
     STAGE(ST_RED, launch_reduce(ctx->partials.as<double>(), r.n_cta, L.size(), ctx->out.as<double>(), ctx->stream));
-    std::vector<double> h(L.size());
-    int hc[4] = {0, 0, 0, 0};
-    CK(cudaMemcpyAsync(h.data(), ctx->out.p, L.size() * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-    CK(cudaMemcpyAsync(hc, ctx->counters.p, 4 * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    const size_t need = L.size() + 2;   // the sums, then 4 ints of counters
+    if (need > ctx->h_out_cap) {
+        if (ctx->h_out) cudaFreeHost(ctx->h_out);
+        ctx->h_out = nullptr;
+        ctx->h_out_cap = 0;
+        CKM(cudaMallocHost(&ctx->h_out, need * sizeof(double)));
+        ctx->h_out_cap = need;
+    }
+    CK(cudaMemcpyAsync(ctx->h_out, ctx->out.p, L.size() * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->h_out + L.size(), ctx->counters.p, 4 * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     ctx->d2h += L.size() * sizeof(double) + 4 * sizeof(int);
+    if (int r1 = stage_end(ctx, r.run_ev)) return r1;
+    return 0;
+}
+
+// Phase 3b: wait for the context's stream and hand out the results.
+int finish_collect(mepi_ctx* ctx, mepi_acc* out) {
+    mepi_ctx::Run& r = ctx->run;
+    const mepi_job& job = r.job;
+    const AccLayout& L = r.L;
+    int rc = 0;
+    CK(cudaStreamSynchronize(ctx->stream));
     if (r.perk && r.count > 0) {
-        CK(cudaMemcpyAsync(out->perk, ctx->perk.p, r.count * 4 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaMemcpy(out->perk, ctx->perk.p, r.count * 4 * sizeof(double), cudaMemcpyDeviceToHost));
         ctx->d2h += r.count * 4 * sizeof(double);
     }
-    if (int r1 = stage_end(ctx, r.run_ev)) return r1;
-    CK(cudaStreamSynchronize(ctx->stream));
+    const double* h = ctx->h_out;
+    int hc[4];
+    std::memcpy(hc, h + L.size(), sizeof(hc));
     CK(cudaGetLastError());
     if (ctx->tc.err) {
         int terr = 0;
@@ -658,7 +682,7 @@ int run_finish(mepi_ctx* ctx, mepi_acc* out) {
     if (rc) return rc;
     const int nE = job.n_eF, nv = job.valence_bands;
     auto put = [&](double* dst, int off, int n) {
-        if (dst) std::memcpy(dst, h.data() + off, n * sizeof(double));
+        if (dst) std::memcpy(dst, h + off, n * sizeof(double));
     };
     put(out->Ne_sum, L.ne_off(), nE);
     put(out->ahc, L.ahc_off(), 9 * nE);
@@ -673,7 +697,7 @@ int run_finish(mepi_ctx* ctx, mepi_acc* out) {
         put(out->kubo_ohc, L.koh_off(), 18 * r.n_hw * nE);
     }
     out->n_k_done = r.count;
-    out->n_k_fp64 = r.fp64 ? r.count : (int64_t)redo.size();
+    out->n_k_fp64 = r.fp64 ? r.count : r.n_redo;
     out->eig_max_sweeps = hc[0];
     // counters[1] counts FP64 Jacobi launches that hit the sweep cap (an error);
     // FP32 cap hits (counters[2]) were flagged and rerun in FP64.
@@ -684,7 +708,8 @@ int run_finish(mepi_ctx* ctx, mepi_acc* out) {
 int run_impl(mepi_ctx* ctx, const mepi_job* job, mepi_acc* out) {
     int rc = run_prepare(ctx, job, out);
     if (!rc) rc = run_enqueue(ctx);
-    if (!rc) rc = run_finish(ctx, out);
+    if (!rc) rc = finish_enqueue(ctx);
+    if (!rc) rc = finish_collect(ctx, out);
     return rc;
 }
 
@@ -1157,9 +1182,14 @@ int mepi_run_batch(int32_t n, mepi_ctx* const* ctxs, const mepi_job* jobs, mepi_
         float ms = 0.f;
         if (cudaEventElapsedTime(&ms, t0, t1) != cudaSuccess) return cleanup(MEPI_ERR_CUDA);
         if (graph_ms) *graph_ms = ms;
-        // 4. reruns, reductions and copies back, per context
+        // 4. reruns, reductions and copies back: enqueued for every context
+        //    first, so that the contexts' reruns overlap, then collected
         for (int i = 0; i < n; ++i) {
-            rc = run_finish(ctxs[i], &accs[i]);
+            rc = finish_enqueue(ctxs[i]);
+            if (rc) return cleanup(rc);
+        }
+        for (int i = 0; i < n; ++i) {
+            rc = finish_collect(ctxs[i], &accs[i]);
             if (rc) return cleanup(rc);
         }
         return cleanup(MEPI_OK);
@@ -1184,6 +1214,7 @@ int mepi_destroy(mepi_ctx* ctx) {
         cudaEventDestroy(ev.b);
     }
     if (ctx->h_flags) cudaFreeHost(ctx->h_flags);
+    if (ctx->h_out) cudaFreeHost(ctx->h_out);
     tc_plan_free(ctx->tc);
     sep_plan_free(ctx->sep);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);

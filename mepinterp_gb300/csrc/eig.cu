@@ -44,6 +44,13 @@ __device__ __forceinline__ T cta_sum(T v, T* red) {
     return s;
 }
 
+// Rotation of one pair of a round, packed so that a thread fetches it with
+// one vector load (c, s, e^{i phi}) plus one for the indices.
+template <typename T>
+struct alignas(4 * sizeof(T)) RotPar {
+    T c, s, pr, pi;
+};
+
 // One CTA diagonalises a run of kblock consecutive k-points.  The matrix M
 // and the eigenvector accumulator V live in shared memory as separate real
 // and imaginary planes with row stride NP + 1 (NP = the band count padded to
@@ -67,8 +74,10 @@ __global__ void __launch_bounds__(256) jacobi_kernel(int N, int64_t nk, int kblo
     T* Vi = Vr + PL;
     T* Tr = Vi + PL;  // warm-start product / sorted eigenvectors
     T* Ti = Tr + PL;
-    __shared__ T s_c[HP], s_s[HP], s_pr[HP], s_pi[HP], s_d0[HP], s_d1[HP];
-    __shared__ int s_p[HP], s_q[HP], s_fix[HP];
+    __shared__ RotPar<T> s_rot[HP];
+    __shared__ int2 s_pq[HP];
+    __shared__ T s_d0[HP], s_d1[HP];
+    __shared__ int s_fix[HP];
     __shared__ T red[8];
     __shared__ T s_E[NP];
     const int tid = threadIdx.x, nt = blockDim.x;
@@ -189,16 +198,19 @@ __global__ void __launch_bounds__(256) jacobi_kernel(int N, int64_t nk, int kblo
                             fix = 1;
                         }
                     }
-                    s_p[tid] = p; s_q[tid] = q; s_c[tid] = c; s_s[tid] = sn; s_pr[tid] = pr; s_pi[tid] = pi;
+                    s_pq[tid] = make_int2(p, q);
+                    s_rot[tid] = RotPar<T>{c, sn, pr, pi};
                     s_d0[tid] = d0; s_d1[tid] = d1; s_fix[tid] = fix;
                 }
                 __syncthreads();
                 // 2. M <- G^dag M G, one 2 x 2 block per (pair A, pair B)
                 for (int t = tid; t < HP * HP; t += nt) {
                     const int A = t / HP, B = t % HP;
-                    const int pA = s_p[A], qA = s_q[A], pB = s_p[B], qB = s_q[B];
-                    const T cA = s_c[A], sA = s_s[A], cB = s_c[B], sB = s_s[B];
-                    const cplx<T> phA = mk(s_pr[A], s_pi[A]), phB = mk(s_pr[B], s_pi[B]);
+                    const int2 pqA = s_pq[A], pqB = s_pq[B];
+                    const int pA = pqA.x, qA = pqA.y, pB = pqB.x, qB = pqB.y;
+                    const RotPar<T> rA = s_rot[A], rB = s_rot[B];
+                    const T cA = rA.c, sA = rA.s, cB = rB.c, sB = rB.s;
+                    const cplx<T> phA = mk(rA.pr, rA.pi), phB = mk(rB.pr, rB.pi);
                     const cplx<T> x00 = mk(Mr[pA * LD + pB], Mi[pA * LD + pB]), x01 = mk(Mr[pA * LD + qB], Mi[pA * LD + qB]);
                     const cplx<T> x10 = mk(Mr[qA * LD + pB], Mi[qA * LD + pB]), x11 = mk(Mr[qA * LD + qB], Mi[qA * LD + qB]);
                     // Y = X G_B: column p' = c xp - s e^{-i phi} xq ; column q' = s e^{i phi} xp + c xq
@@ -221,9 +233,11 @@ __global__ void __launch_bounds__(256) jacobi_kernel(int N, int64_t nk, int kblo
                 // 3. V <- V G (consecutive threads walk the rows of one pair)
                 for (int t = tid; t < NP * HP; t += nt) {
                     const int j = t / NP, i = t % NP;
-                    const int p = s_p[j], q = s_q[j];
-                    const T c = s_c[j], sn = s_s[j];
-                    const cplx<T> ph = mk(s_pr[j], s_pi[j]);
+                    const int2 pq = s_pq[j];
+                    const int p = pq.x, q = pq.y;
+                    const RotPar<T> rj = s_rot[j];
+                    const T c = rj.c, sn = rj.s;
+                    const cplx<T> ph = mk(rj.pr, rj.pi);
                     const cplx<T> vp = mk(Vr[i * LD + p], Vi[i * LD + p]), vq = mk(Vr[i * LD + q], Vi[i * LD + q]);
                     const cplx<T> np_ = c * vp - sn * mul_cj(vq, ph), nq = sn * (ph * vp) + c * vq;
                     Vr[i * LD + p] = np_.re; Vi[i * LD + p] = np_.im;

@@ -118,17 +118,37 @@ __device__ void load_items(ItemHead<TG, KI>& h, const KRange& kr, int nbz, int r
         for (int it = 1; it < h.n_items; ++it) u &= (h.slab[it] == h.slab[0]) ? 1 : 0;
         h.uniform = u;
     }
+    // phases: FP64 for FP64 slabs; for FP32 slabs the angle is reduced to
+    // [-1, 1] (units of pi) in FP64 and its sine and cosine taken in FP32
     for (int e = threadIdx.x; e < KI * 32; e += blockDim.x) {
         const int it = e / 32, iz = e % 32;
-        const cplx<double> p = iz < nbz ? phase(h.k[it][2], rz0 + iz) : mk(0.0, 0.0);
-        h.ph[it][iz] = mk((TG)p.re, (TG)p.im);
+        if constexpr (sizeof(TG) == 4) {
+            float sn = 0.f, cs = 0.f;
+            if (iz < nbz) {
+                double x = 2.0 * h.k[it][2] * (double)(rz0 + iz);
+                x -= 2.0 * rint(0.5 * x);
+                sincospif((float)x, &sn, &cs);
+            }
+            h.ph[it][iz] = mk((TG)cs, (TG)sn);
+        } else {
+            const cplx<double> p = iz < nbz ? phase(h.k[it][2], rz0 + iz) : mk(0.0, 0.0);
+            h.ph[it][iz] = mk((TG)p.re, (TG)p.im);
+        }
     }
     if (tau)
         for (int e = threadIdx.x; e < KI * N; e += blockDim.x) {
             const int it = e / N, n = e % N;
-            double s, c;
-            sincospi(2.0 * (h.k[it][0] * tau[3 * n] + h.k[it][1] * tau[3 * n + 1] + h.k[it][2] * tau[3 * n + 2]), &s, &c);
-            h.phi[it][n] = mk((TG)c, (TG)s);
+            double x = 2.0 * (h.k[it][0] * tau[3 * n] + h.k[it][1] * tau[3 * n + 1] + h.k[it][2] * tau[3 * n + 2]);
+            if constexpr (sizeof(TG) == 4) {
+                x -= 2.0 * rint(0.5 * x);
+                float sn, cs;
+                sincospif((float)x, &sn, &cs);
+                h.phi[it][n] = mk((TG)cs, (TG)sn);
+            } else {
+                double sn, cs;
+                sincospi(x, &sn, &cs);
+                h.phi[it][n] = mk((TG)cs, (TG)sn);
+            }
         }
     __syncthreads();
 }
@@ -172,69 +192,71 @@ __global__ void __launch_bounds__(128) sep_w_kernel(DevModel m, KRange kr, const
     const int NN = m.N * m.N, PT = blockDim.x, t = threadIdx.x;
     load_items<TG, KI>(h, kr, nbz, rz0, (size_t)nbz * NB * NN, m.has_tau ? m.tau : nullptr, m.N, qx0, nqx);
     // every block is Hermitian and its consumers read the upper triangle:
-    // threads walk the N (N + 1) / 2 elements n <= m
-    const int u = blockIdx.y * PT + t;
-    if (u >= m.N * (m.N + 1) / 2) return;
-    int n, mm;
-    upper_pair(u, m.N, n, mm);
-    const int pair = n * m.N + mm;
-    TG dt[3] = {(TG)0, (TG)0, (TG)0};
-    cplx<TG> psi[KI];
+    // the CTA walks the N (N + 1) / 2 elements n <= m in tiles of PT, so the
+    // item header above is formed once per KI items
+    const int NU = m.N * (m.N + 1) / 2;
+    for (int u = t; u < NU; u += PT) {
+        int n, mm;
+        upper_pair(u, m.N, n, mm);
+        const int pair = n * m.N + mm;
+        TG dt[3] = {(TG)0, (TG)0, (TG)0};
+        cplx<TG> psi[KI];
 #pragma unroll
-    for (int it = 0; it < KI; ++it) psi[it] = mk((TG)1, (TG)0);
-    if (m.has_tau) {
-        double d[3];
+        for (int it = 0; it < KI; ++it) psi[it] = mk((TG)1, (TG)0);
+        if (m.has_tau) {
+            double d[3];
 #pragma unroll
-        for (int i = 0; i < 3; ++i) d[i] = m.tau[mm * 3 + i] - m.tau[n * 3 + i];
+            for (int i = 0; i < 3; ++i) d[i] = m.tau[mm * 3 + i] - m.tau[n * 3 + i];
 #pragma unroll
-        for (int a = 0; a < 3; ++a) dt[a] = (TG)(m.C[a * 3 + 0] * d[0] + m.C[a * 3 + 1] * d[1] + m.C[a * 3 + 2] * d[2]);
+            for (int a = 0; a < 3; ++a) dt[a] = (TG)(m.C[a * 3 + 0] * d[0] + m.C[a * 3 + 1] * d[1] + m.C[a * 3 + 2] * d[2]);
 #pragma unroll
-        for (int it = 0; it < KI; ++it) psi[it] = cj_mul(h.phi[it][n], h.phi[it][mm]);
-    }
-    const int64_t i0 = (int64_t)blockIdx.x * KI;
-    auto Wp = [&](int it, int b) { return W + ((size_t)(i0 + it) * NB + b) * NN + pair; };
-    auto Xp = [&](int slot, int it) -> cplx<TG>& { return Xs[((size_t)slot * KI + it) * PT + t]; };
-    cplx<TG> acc[KI];
-    // H, then the connection A_b
-    column_sum<TG, KI>(h, G2 + pair, (size_t)NB * NN, nbz, acc);
-#pragma unroll
-    for (int it = 0; it < KI; ++it) {
-        const cplx<TG> v = psi[it] * acc[it];
-        Xp(0, it) = v;
-        if (sizeof(T) == 8 && it < h.n_items) *Wp(it, 0) = mk((T)v.re, (T)v.im);
-    }
-    if constexpr (NB == 10) {
-#pragma unroll
-        for (int b = 0; b < 3; ++b) {
-            column_sum<TG, KI>(h, G2 + (size_t)(4 + b) * NN + pair, (size_t)NB * NN, nbz, acc);
-#pragma unroll
-            for (int it = 0; it < KI; ++it) {
-                const cplx<TG> v = psi[it] * acc[it];
-                Xp(1 + b, it) = v;
-                if (it < h.n_items) *Wp(it, 4 + b) = mk((T)v.re, (T)v.im);
-            }
+            for (int it = 0; it < KI; ++it) psi[it] = cj_mul(h.phi[it][n], h.phi[it][mm]);
         }
-    }
-    // H_a
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        column_sum<TG, KI>(h, G2 + (size_t)(1 + a) * NN + pair, (size_t)NB * NN, nbz, acc);
+        const int64_t i0 = (int64_t)blockIdx.x * KI;
+        auto Wp = [&](int it, int b) { return W + ((size_t)(i0 + it) * NB + b) * NN + pair; };
+        auto Xp = [&](int slot, int it) -> cplx<TG>& { return Xs[((size_t)slot * KI + it) * PT + t]; };
+        cplx<TG> acc[KI];
+        // H, then the connection A_b
+        column_sum<TG, KI>(h, G2 + pair, (size_t)NB * NN, nbz, acc);
 #pragma unroll
         for (int it = 0; it < KI; ++it) {
-            const cplx<TG> v = times_i(psi[it] * acc[it] + dt[a] * Xp(0, it));
-            if (it < h.n_items) *Wp(it, 1 + a) = mk((T)v.re, (T)v.im);
+            const cplx<TG> v = psi[it] * acc[it];
+            Xp(0, it) = v;
+            if (sizeof(T) == 8 && it < h.n_items) *Wp(it, 0) = mk((T)v.re, (T)v.im);
         }
-    }
-    // Omega_q, q = (x,y), (x,z), (y,z)
-    if constexpr (NB == 10) {
-        constexpr int qa[3] = {0, 0, 1}, qb[3] = {1, 2, 2};
+        if constexpr (NB == 10) {
 #pragma unroll
-        for (int q = 0; q < 3; ++q) {
-            column_sum<TG, KI>(h, G2 + (size_t)(7 + q) * NN + pair, (size_t)NB * NN, nbz, acc);
+            for (int b = 0; b < 3; ++b) {
+                column_sum<TG, KI>(h, G2 + (size_t)(4 + b) * NN + pair, (size_t)NB * NN, nbz, acc);
+#pragma unroll
+                for (int it = 0; it < KI; ++it) {
+                    const cplx<TG> v = psi[it] * acc[it];
+                    Xp(1 + b, it) = v;
+                    if (it < h.n_items) *Wp(it, 4 + b) = mk((T)v.re, (T)v.im);
+                }
+            }
+        }
+        // H_a
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            column_sum<TG, KI>(h, G2 + (size_t)(1 + a) * NN + pair, (size_t)NB * NN, nbz, acc);
 #pragma unroll
             for (int it = 0; it < KI; ++it) {
-                const cplx<TG> v = times_i(psi[it] * acc[it] + dt[qa[q]] * Xp(1 + qb[q], it) - dt[qb[q]] * Xp(1 + qa[q], it));
-                if (it < h.n_items) *Wp(it, 7 + q) = mk((T)v.re, (T)v.im);
+                const cplx<TG> v = times_i(psi[it] * acc[it] + dt[a] * Xp(0, it));
+                if (it < h.n_items) *Wp(it, 1 + a) = mk((T)v.re, (T)v.im);
+            }
+        }
+        // Omega_q, q = (x,y), (x,z), (y,z)
+        if constexpr (NB == 10) {
+            constexpr int qa[3] = {0, 0, 1}, qb[3] = {1, 2, 2};
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                column_sum<TG, KI>(h, G2 + (size_t)(7 + q) * NN + pair, (size_t)NB * NN, nbz, acc);
+#pragma unroll
+                for (int it = 0; it < KI; ++it) {
+                    const cplx<TG> v = times_i(psi[it] * acc[it] + dt[qa[q]] * Xp(1 + qb[q], it) - dt[qb[q]] * Xp(1 + qa[q], it));
+                    if (it < h.n_items) *Wp(it, 7 + q) = mk((T)v.re, (T)v.im);
+                }
             }
         }
     }
@@ -297,54 +319,55 @@ __global__ void __launch_bounds__(128) sep_h64_df_kernel(const cplx<double>* __r
             split_d(h.phi[it][n].im, fih[it][n].im, fil[it][n].im);
         }
     __syncthreads();
-    const int u = blockIdx.y * blockDim.x + threadIdx.x;
-    if (u >= N * (N + 1) / 2) return;
-    int n, mm;
-    upper_pair(u, N, n, mm);
-    const int pair = n * N + mm;
     const size_t zs = (size_t)nbd * NN;
-    DFc acc[KI];
+    const int NU = N * (N + 1) / 2;
+    for (int u = threadIdx.x; u < NU; u += blockDim.x) {
+        int n, mm;
+        upper_pair(u, N, n, mm);
+        const int pair = n * N + mm;
+        DFc acc[KI];
 #pragma unroll
-    for (int it = 0; it < KI; ++it) acc[it] = DFc{DF{0.f, 0.f}, DF{0.f, 0.f}};
-    if (h.uniform) {
-        const cplx<double>* gp = G2 + pair + h.slab[0];
-        for (int iz = 0; iz < nbz; ++iz) {
-            const cplx<double> v = gp[(size_t)iz * zs];
-            cplx<float> vh, vl;
-            split_d(v.re, vh.re, vl.re);
-            split_d(v.im, vh.im, vl.im);
+        for (int it = 0; it < KI; ++it) acc[it] = DFc{DF{0.f, 0.f}, DF{0.f, 0.f}};
+        if (h.uniform) {
+            const cplx<double>* gp = G2 + pair + h.slab[0];
+            for (int iz = 0; iz < nbz; ++iz) {
+                const cplx<double> v = gp[(size_t)iz * zs];
+                cplx<float> vh, vl;
+                split_d(v.re, vh.re, vl.re);
+                split_d(v.im, vh.im, vl.im);
 #pragma unroll
-            for (int it = 0; it < KI; ++it) dfc_mac(acc[it], phh[it][iz], phl[it][iz], vh, vl);
+                for (int it = 0; it < KI; ++it) dfc_mac(acc[it], phh[it][iz], phl[it][iz], vh, vl);
+            }
+        } else {
+#pragma unroll
+            for (int it = 0; it < KI; ++it)
+                if (it < h.n_items)
+                    for (int iz = 0; iz < nbz; ++iz) {
+                        const cplx<double> v = G2[pair + h.slab[it] + (size_t)iz * zs];
+                        cplx<float> vh, vl;
+                        split_d(v.re, vh.re, vl.re);
+                        split_d(v.im, vh.im, vl.im);
+                        dfc_mac(acc[it], phh[it][iz], phl[it][iz], vh, vl);
+                    }
         }
-    } else {
+        const int64_t i0 = (int64_t)blockIdx.x * KI;
 #pragma unroll
-        for (int it = 0; it < KI; ++it)
-            if (it < h.n_items)
-                for (int iz = 0; iz < nbz; ++iz) {
-                    const cplx<double> v = G2[pair + h.slab[it] + (size_t)iz * zs];
-                    cplx<float> vh, vl;
-                    split_d(v.re, vh.re, vl.re);
-                    split_d(v.im, vh.im, vl.im);
-                    dfc_mac(acc[it], phh[it][iz], phl[it][iz], vh, vl);
-                }
-    }
-    const int64_t i0 = (int64_t)blockIdx.x * KI;
-#pragma unroll
-    for (int it = 0; it < KI; ++it) {
-        if (it >= h.n_items) break;
-        DFc r = acc[it];
-        if (tau) {
-            // psi = conj(phi_n) phi_m, then psi * X
-            const cplx<float> an_h = conjg(fih[it][n]), an_l = conjg(fil[it][n]);
-            DFc ps{DF{0.f, 0.f}, DF{0.f, 0.f}};
-            dfc_mac(ps, an_h, an_l, fih[it][mm], fil[it][mm]);
-            cplx<float> psh, psl, xh, xl;
-            dfc_split(ps, psh, psl);
-            dfc_split(r, xh, xl);
-            r = DFc{DF{0.f, 0.f}, DF{0.f, 0.f}};
-            dfc_mac(r, psh, psl, xh, xl);
+        for (int it = 0; it < KI; ++it) {
+            if (it >= h.n_items) break;
+            DFc r = acc[it];
+            if (tau) {
+                // psi = conj(phi_n) phi_m, then psi * X
+                const cplx<float> an_h = conjg(fih[it][n]), an_l = conjg(fil[it][n]);
+                DFc ps{DF{0.f, 0.f}, DF{0.f, 0.f}};
+                dfc_mac(ps, an_h, an_l, fih[it][mm], fil[it][mm]);
+                cplx<float> psh, psl, xh, xl;
+                dfc_split(ps, psh, psl);
+                dfc_split(r, xh, xl);
+                r = DFc{DF{0.f, 0.f}, DF{0.f, 0.f}};
+                dfc_mac(r, psh, psl, xh, xl);
+            }
+            H64[(size_t)(i0 + it) * NN + pair] = mk((double)r.re.s + (double)r.re.c, (double)r.im.s + (double)r.im.c);
         }
-        H64[(size_t)(i0 + it) * NN + pair] = mk((double)r.re.s + (double)r.re.c, (double)r.im.s + (double)r.im.c);
     }
 }
 
@@ -486,8 +509,8 @@ cudaError_t launch_w(const DevModel& m, const KRange& kr, const cplx<TG>* G2, in
     cudaError_t e = cudaFuncSetAttribute(sep_w_kernel<T, TG, NB, KI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
     if (e != cudaSuccess) return e;
-    dim3 grid((unsigned)((kr.count + KI - 1) / KI), (unsigned)((NU + PT - 1) / PT));
-    sep_w_kernel<T, TG, NB, KI><<<grid, PT, smem, s>>>(m, kr, G2, nbz, rz0, qx0, nqx, W);
+    sep_w_kernel<T, TG, NB, KI><<<(unsigned)((kr.count + KI - 1) / KI), PT, smem, s>>>(m, kr, G2, nbz, rz0, qx0, nqx,
+                                                                                      W);
     return cudaGetLastError();
 }
 }  // namespace
@@ -495,9 +518,8 @@ cudaError_t launch_w(const DevModel& m, const KRange& kr, const cplx<TG>* G2, in
 cudaError_t launch_sep_h64(const SepPlan& p, const KRange& kr, cplx<double>* H64, cudaStream_t s) {
     if (kr.count <= 0) return cudaSuccess;
     const int NU = p.N * (p.N + 1) / 2, PT = pair_tile(NU);
-    dim3 grid((unsigned)((kr.count + kItemsH - 1) / kItemsH), (unsigned)((NU + PT - 1) / PT));
-    sep_h64_df_kernel<kItemsH><<<grid, PT, 0, s>>>(p.G2d, kr, p.N, p.nbd, p.nb[2], p.lo[2], p.tau, p.built_qx0,
-                                                   p.nqx, H64);
+    sep_h64_df_kernel<kItemsH><<<(unsigned)((kr.count + kItemsH - 1) / kItemsH), PT, 0, s>>>(
+        p.G2d, kr, p.N, p.nbd, p.nb[2], p.lo[2], p.tau, p.built_qx0, p.nqx, H64);
     return cudaGetLastError();
 }
 
