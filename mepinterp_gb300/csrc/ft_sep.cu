@@ -118,37 +118,19 @@ __device__ void load_items(ItemHead<TG, KI>& h, const KRange& kr, int nbz, int r
         for (int it = 1; it < h.n_items; ++it) u &= (h.slab[it] == h.slab[0]) ? 1 : 0;
         h.uniform = u;
     }
-    // phases: FP64 for FP64 slabs; for FP32 slabs the angle is reduced to
-    // [-1, 1] (units of pi) in FP64 and its sine and cosine taken in FP32
+    // phases in FP64 (rounded once to TG): formed once per CTA of KI items
     for (int e = threadIdx.x; e < KI * 32; e += blockDim.x) {
         const int it = e / 32, iz = e % 32;
-        if constexpr (sizeof(TG) == 4) {
-            float sn = 0.f, cs = 0.f;
-            if (iz < nbz) {
-                double x = 2.0 * h.k[it][2] * (double)(rz0 + iz);
-                x -= 2.0 * rint(0.5 * x);
-                sincospif((float)x, &sn, &cs);
-            }
-            h.ph[it][iz] = mk((TG)cs, (TG)sn);
-        } else {
-            const cplx<double> p = iz < nbz ? phase(h.k[it][2], rz0 + iz) : mk(0.0, 0.0);
-            h.ph[it][iz] = mk((TG)p.re, (TG)p.im);
-        }
+        const cplx<double> p = iz < nbz ? phase(h.k[it][2], rz0 + iz) : mk(0.0, 0.0);
+        h.ph[it][iz] = mk((TG)p.re, (TG)p.im);
     }
     if (tau)
         for (int e = threadIdx.x; e < KI * N; e += blockDim.x) {
             const int it = e / N, n = e % N;
-            double x = 2.0 * (h.k[it][0] * tau[3 * n] + h.k[it][1] * tau[3 * n + 1] + h.k[it][2] * tau[3 * n + 2]);
-            if constexpr (sizeof(TG) == 4) {
-                x -= 2.0 * rint(0.5 * x);
-                float sn, cs;
-                sincospif((float)x, &sn, &cs);
-                h.phi[it][n] = mk((TG)cs, (TG)sn);
-            } else {
-                double sn, cs;
-                sincospi(x, &sn, &cs);
-                h.phi[it][n] = mk((TG)cs, (TG)sn);
-            }
+            double sn, cs;
+            sincospi(2.0 * (h.k[it][0] * tau[3 * n] + h.k[it][1] * tau[3 * n + 1] + h.k[it][2] * tau[3 * n + 2]), &sn,
+                     &cs);
+            h.phi[it][n] = mk((TG)cs, (TG)sn);
         }
     __syncthreads();
 }
