@@ -459,7 +459,9 @@ def run_batched(args, rank, world):
         seq_dev_ms += c.timing()["run_ms"]
         c.trim()
     seq_s = time.perf_counter() - t0
-    diff = max(_rel_max(a[k], b[k]) for a, b in zip(res, seq) for k in ("ahc", "mep_ic", "kubo_mep_ic"))
+    diffs = [(_rel_max(a[k], b[k]), i, k) for i, (a, b) in enumerate(zip(res, seq))
+             for k in ("ahc", "mep_ic", "kubo_mep_ic")]
+    diff, worst_model, worst_key = max(diffs)
     for c in ctxs:
         c.close()
     value = nk * args.steps / sum(wall)
@@ -476,7 +478,7 @@ def run_batched(args, rank, world):
         "graph_value": nk / (statistics.median(graph) * 1e-3),
         "sequential": {"value": nk / seq_s, "device_value": nk / (seq_dev_ms * 1e-3), "seconds": seq_s},
         "speedup_vs_sequential": (nk / (sum(wall) / args.steps)) / (nk / seq_s),
-        "batch_vs_sequential_max_rel_diff": diff,
+        "batch_vs_sequential_max_rel_diff": {"value": diff, "model": worst_model, "key": worst_key},
         "create_s": create_s, "autotune_s": tune_s, "clocks": clk,
     }
     if rank == 0:

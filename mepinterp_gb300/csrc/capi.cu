@@ -106,6 +106,10 @@ struct mepi_ctx {
         size_t run_ev = 0;
         bool perk = false;              // per-k output requested
         int64_t n_redo = 0;             // k-points rerun in FP64
+        // the FP64 reruns between finish_prepare and finish_launch
+        std::vector<int64_t> redo, redo_pos, rslab;
+        int64_t rchunk = 0;
+        bool sep_keep = false;
     } run;
     double* h_out = nullptr;            // pinned copy-back of the reduced sums and counters
     size_t h_out_cap = 0;
@@ -572,32 +576,35 @@ int enqueue_range(mepi_ctx* ctx, int64_t b, int64_t e) {
     return 0;
 }
 
-// Phase 3a: the FP64 reruns of the mixed form, the fixed-order reduction and
-// the asynchronous copy back into pinned memory.  The batched form enqueues
-// this for every context before collecting any, so the contexts' reruns
-// overlap on the GPU.
-int finish_enqueue(mepi_ctx* ctx) {
+// Phase 3: the FP64 reruns of the mixed form, the fixed-order reduction and
+// the copy back.  3a (finish_prepare) reads the rerun flags and makes every
+// allocation and plan the reruns need; 3b (finish_launch) enqueues the
+// reruns, the reduction and the asynchronous copy back into pinned memory;
+// 3c (finish_collect) waits and hands out the results.  The batched form runs
+// 3a for every context, then 3b for every context (no allocation there, so no
+// implicit device-wide synchronisation: the contexts' reruns overlap on the
+// GPU), then 3c.
+int finish_prepare(mepi_ctx* ctx) {
     mepi_ctx::Run& r = ctx->run;
     const mepi_job& job = r.job;
-    const AccLayout& L = r.L;
-    std::vector<int64_t> redo, redo_pos;
-    int rc = 0;
+    r.redo.clear();
+    r.redo_pos.clear();
+    r.rslab.clear();
+    r.sep_keep = ctx->sep_active;
     if (!r.fp64) {
         CK(cudaStreamSynchronize(ctx->stream));
         for (int64_t i = 0; i < r.count; ++i)
             if (ctx->h_flags[i]) {
-                redo.push_back(ctx->sep_active ? ctx->kcol_host[i]
-                               : job.k_list    ? job.k_list[i]
-                                               : job.k_begin + i * job.k_stride);
-                redo_pos.push_back(ctx->sep_active ? ctx->kpos_host[i] : i);
+                r.redo.push_back(ctx->sep_active ? ctx->kcol_host[i]
+                                 : job.k_list    ? job.k_list[i]
+                                                 : job.k_begin + i * job.k_stride);
+                r.redo_pos.push_back(ctx->sep_active ? ctx->kpos_host[i] : i);
             }
         // A slabbed mixed plan holds FP32 slabs of one qx range: the reruns get
         // FP64 slabs of every block instead, built over their own qx ranges
         // (the reruns are in column order, qx-outermost); the next run rebuilds
         // its plan.  Where no FP64 slab fits, the reruns take the direct sums.
-        const bool sep_keep = ctx->sep_active;
-        std::vector<int64_t> rslab;
-        if (!redo.empty() && ctx->sep_active && !ctx->sep.whole()) {
+        if (!r.redo.empty() && ctx->sep_active && !ctx->sep.whole()) {
             const int mp[3] = {job.mp_grid[0], job.mp_grid[1], job.mp_grid[2]};
             sep_plan_free(ctx->sep);
             const int prc = sep_plan_build(ctx->sep, ctx->dm, ctx->R_host.data(), ctx->S_host.data(), mp, true,
@@ -607,43 +614,25 @@ int finish_enqueue(mepi_ctx* ctx) {
                 return prc;
             }
             if (prc == 0) ctx->h2d += ctx->sep.h2d_bytes;
-            if (prc == 0 && !ctx->sep.whole()) slab_ranges(redo.data(), (int64_t)redo.size(), mp[0], ctx->sep.nqx, rslab);
+            if (prc == 0 && !ctx->sep.whole())
+                slab_ranges(r.redo.data(), (int64_t)r.redo.size(), mp[0], ctx->sep.nqx, r.rslab);
         }
-        if (!ctx->sep.ready || (!ctx->sep.whole() && rslab.empty())) ctx->sep_active = false;
-        if (!redo.empty()) {
-            int64_t rchunk =
-                std::min<int64_t>(default_chunk(ctx->N, ctx->nb, true, ctx->mem_budget), (int64_t)redo.size());
-            rc = ensure_chunk<double>(ctx, rchunk);
-            if (rc) return rc;
-            CKM(ctx->klist.ensure(redo.size() * sizeof(int64_t)));
-            CK(cudaMemcpyAsync(ctx->klist.p, redo.data(), redo.size() * sizeof(int64_t), cudaMemcpyHostToDevice,
+        if (!r.redo.empty()) {
+            r.rchunk = std::min<int64_t>(default_chunk(ctx->N, ctx->nb, true, ctx->mem_budget), (int64_t)r.redo.size());
+            if (int rc = ensure_chunk<double>(ctx, r.rchunk)) return rc;
+            CKM(ctx->klist.ensure(r.redo.size() * sizeof(int64_t)));
+            CK(cudaMemcpyAsync(ctx->klist.p, r.redo.data(), r.redo.size() * sizeof(int64_t), cudaMemcpyHostToDevice,
                                ctx->stream));
-            ctx->h2d += redo.size() * sizeof(int64_t);
+            ctx->h2d += r.redo.size() * sizeof(int64_t);
             if (r.perk) {
-                CKM(ctx->rpos.ensure(redo_pos.size() * sizeof(int64_t)));
-                CK(cudaMemcpyAsync(ctx->rpos.p, redo_pos.data(), redo_pos.size() * sizeof(int64_t),
+                CKM(ctx->rpos.ensure(r.redo_pos.size() * sizeof(int64_t)));
+                CK(cudaMemcpyAsync(ctx->rpos.p, r.redo_pos.data(), r.redo_pos.size() * sizeof(int64_t),
                                    cudaMemcpyHostToDevice, ctx->stream));
             }
-            if (rslab.empty()) rslab = {0, (int64_t)redo.size()};
-            for (size_t j = 0; j + 1 < rslab.size(); ++j) {
-                const int64_t b = rslab[j], e = rslab[j + 1];
-                if (e <= b) continue;
-                if (ctx->sep_active && !ctx->sep.whole())
-                    STAGE(ST_FT, launch_sep_slab(ctx->sep, (int)j * ctx->sep.nqx, ctx->stream));
-                for (int64_t c0 = b; c0 < e; c0 += rchunk) {
-                    KRange kr{0, 1, std::min<int64_t>(rchunk, e - c0), ctx->klist.as<int64_t>() + c0, nullptr,
-                              {job.mp_grid[0], job.mp_grid[1], job.mp_grid[2]}};
-                    rc = run_chunk<double>(ctx, kr, &r.jb, r.n_cta, 0.0, false, true, nullptr);
-                    if (!rc && r.perk) rc = enqueue_perk<double>(ctx, kr.count, ctx->rpos.as<int64_t>() + c0, 0);
-                    if (rc) return rc;
-                }
-            }
         }
-        ctx->sep_active = sep_keep;
     }
-    r.n_redo = (int64_t)redo.size();
-    STAGE(ST_RED, launch_reduce(ctx->partials.as<double>(), r.n_cta, L.size(), ctx->out.as<double>(), ctx->stream));
-    const size_t need = L.size() + 2;   // the sums, then 4 ints of counters
+    r.n_redo = (int64_t)r.redo.size();
+    const size_t need = r.L.size() + 2;   // the sums, then 4 ints of counters
     if (need > ctx->h_out_cap) {
         if (ctx->h_out) cudaFreeHost(ctx->h_out);
         ctx->h_out = nullptr;
@@ -651,6 +640,33 @@ int finish_enqueue(mepi_ctx* ctx) {
         CKM(cudaMallocHost(&ctx->h_out, need * sizeof(double)));
         ctx->h_out_cap = need;
     }
+    return 0;
+}
+
+int finish_launch(mepi_ctx* ctx) {
+    mepi_ctx::Run& r = ctx->run;
+    const mepi_job& job = r.job;
+    const AccLayout& L = r.L;
+    int rc = 0;
+    if (!r.redo.empty()) {
+        if (!ctx->sep.ready || (!ctx->sep.whole() && r.rslab.empty())) ctx->sep_active = false;
+        if (r.rslab.empty()) r.rslab = {0, (int64_t)r.redo.size()};
+        for (size_t j = 0; j + 1 < r.rslab.size(); ++j) {
+            const int64_t b = r.rslab[j], e = r.rslab[j + 1];
+            if (e <= b) continue;
+            if (ctx->sep_active && !ctx->sep.whole())
+                STAGE(ST_FT, launch_sep_slab(ctx->sep, (int)j * ctx->sep.nqx, ctx->stream));
+            for (int64_t c0 = b; c0 < e; c0 += r.rchunk) {
+                KRange kr{0, 1, std::min<int64_t>(r.rchunk, e - c0), ctx->klist.as<int64_t>() + c0, nullptr,
+                          {job.mp_grid[0], job.mp_grid[1], job.mp_grid[2]}};
+                rc = run_chunk<double>(ctx, kr, &r.jb, r.n_cta, 0.0, false, true, nullptr);
+                if (!rc && r.perk) rc = enqueue_perk<double>(ctx, kr.count, ctx->rpos.as<int64_t>() + c0, 0);
+                if (rc) return rc;
+            }
+        }
+        ctx->sep_active = r.sep_keep;
+    }
+    STAGE(ST_RED, launch_reduce(ctx->partials.as<double>(), r.n_cta, L.size(), ctx->out.as<double>(), ctx->stream));
     CK(cudaMemcpyAsync(ctx->h_out, ctx->out.p, L.size() * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaMemcpyAsync(ctx->h_out + L.size(), ctx->counters.p, 4 * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     ctx->d2h += L.size() * sizeof(double) + 4 * sizeof(int);
@@ -658,7 +674,7 @@ int finish_enqueue(mepi_ctx* ctx) {
     return 0;
 }
 
-// Phase 3b: wait for the context's stream and hand out the results.
+// Phase 3c: wait for the context's stream and hand out the results.
 int finish_collect(mepi_ctx* ctx, mepi_acc* out) {
     mepi_ctx::Run& r = ctx->run;
     const mepi_job& job = r.job;
@@ -708,7 +724,8 @@ int finish_collect(mepi_ctx* ctx, mepi_acc* out) {
 int run_impl(mepi_ctx* ctx, const mepi_job* job, mepi_acc* out) {
     int rc = run_prepare(ctx, job, out);
     if (!rc) rc = run_enqueue(ctx);
-    if (!rc) rc = finish_enqueue(ctx);
+    if (!rc) rc = finish_prepare(ctx);
+    if (!rc) rc = finish_launch(ctx);
     if (!rc) rc = finish_collect(ctx, out);
     return rc;
 }
@@ -1182,10 +1199,15 @@ int mepi_run_batch(int32_t n, mepi_ctx* const* ctxs, const mepi_job* jobs, mepi_
         float ms = 0.f;
         if (cudaEventElapsedTime(&ms, t0, t1) != cudaSuccess) return cleanup(MEPI_ERR_CUDA);
         if (graph_ms) *graph_ms = ms;
-        // 4. reruns, reductions and copies back: enqueued for every context
-        //    first, so that the contexts' reruns overlap, then collected
+        // 4. reruns, reductions and copies back: every context's allocations
+        //    first, then every context's launches (they overlap on the GPU),
+        //    then the results
         for (int i = 0; i < n; ++i) {
-            rc = finish_enqueue(ctxs[i]);
+            rc = finish_prepare(ctxs[i]);
+            if (rc) return cleanup(rc);
+        }
+        for (int i = 0; i < n; ++i) {
+            rc = finish_launch(ctxs[i]);
             if (rc) return cleanup(rc);
         }
         for (int i = 0; i < n; ++i) {

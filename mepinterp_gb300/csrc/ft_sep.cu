@@ -173,11 +173,12 @@ __global__ void __launch_bounds__(128) sep_w_kernel(DevModel m, KRange kr, const
     __shared__ ItemHead<TG, KI> h;
     const int NN = m.N * m.N, PT = blockDim.x, t = threadIdx.x;
     load_items<TG, KI>(h, kr, nbz, rz0, (size_t)nbz * NB * NN, m.has_tau ? m.tau : nullptr, m.N, qx0, nqx);
-    // every block is Hermitian and its consumers read the upper triangle:
-    // the CTA walks the N (N + 1) / 2 elements n <= m in tiles of PT, so the
-    // item header above is formed once per KI items
+    // every block is Hermitian and its consumers read the upper triangle: the
+    // CTAs of one item group (blockIdx.y) walk the N (N + 1) / 2 elements n <= m
+    // in tiles of PT, gridDim.y tiles apart (more CTAs keep more of the output
+    // stores in flight; fewer form the item header fewer times)
     const int NU = m.N * (m.N + 1) / 2;
-    for (int u = t; u < NU; u += PT) {
+    for (int u = blockIdx.y * PT + t; u < NU; u += PT * gridDim.y) {
         int n, mm;
         upper_pair(u, m.N, n, mm);
         const int pair = n * m.N + mm;
@@ -491,8 +492,10 @@ cudaError_t launch_w(const DevModel& m, const KRange& kr, const cplx<TG>* G2, in
     cudaError_t e = cudaFuncSetAttribute(sep_w_kernel<T, TG, NB, KI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
     if (e != cudaSuccess) return e;
-    sep_w_kernel<T, TG, NB, KI><<<(unsigned)((kr.count + KI - 1) / KI), PT, smem, s>>>(m, kr, G2, nbz, rz0, qx0, nqx,
-                                                                                      W);
+    // one pair tile per CTA: the kernel streams its W-gauge output, and the
+    // measured time is lowest with the most CTAs in flight
+    dim3 grid((unsigned)((kr.count + KI - 1) / KI), (unsigned)((NU + PT - 1) / PT));
+    sep_w_kernel<T, TG, NB, KI><<<grid, PT, smem, s>>>(m, kr, G2, nbz, rz0, qx0, nqx, W);
     return cudaGetLastError();
 }
 }  // namespace
