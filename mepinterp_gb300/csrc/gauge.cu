@@ -78,18 +78,19 @@ __global__ void __launch_bounds__(256) gauge_kernel(DevModel m, const double* __
     const int nblk = m.has_r ? 6 : 3;
     const cplx<T>* HAk = HA + (size_t)k * 6 * NN;
     g.glob = HAk;
+    const FastDiv byN(N), byNN(NN);
     for (int n = tid; n < N; n += nt) Es[n] = Eg[(size_t)k * N + n];
     for (int e = tid; e < (staged ? nblk * NN : 0); e += nt) {
-        const int blk = e / NN, r = e % NN;
+        const int row = byN.div(e), col = e - row * N;   // row = blk * N + n
         const cplx<T> x = HAk[e];
-        const int o = (blk * N + r / N) * ld + r % N;
+        const int o = row * ld + col;
         g.re[o] = x.re;
         g.im[o] = x.im;
     }
     __syncthreads();
     // inverse gaps of the covariant derivative: the kuboTol decision in FP64
     for (int e = tid; e < NN; e += nt) {
-        const int n = e / N, mm = e % N;
+        const int n = byN.div(e), mm = e - n * N;
         const double ded = Es[mm] - Es[n];
         invd[e] = (m.do_gauge && n != mm && fabs(ded) > m.kubo_tol) ? (T)1 / (T)ded : (T)0;
     }
@@ -97,7 +98,7 @@ __global__ void __launch_bounds__(256) gauge_kernel(DevModel m, const double* __
     cplx<T>* Vk = V + (size_t)k * 3 * NN;
     // velocity
     for (int e = tid; e < 3 * NN; e += nt) {
-        const int a = e / NN, p = (e / N) % N, q = e % N;
+        const int row = byN.div(e), a = byNN.div(e), p = row - a * N, q = e - row * N;
         const cplx<T> hb = g.X(a, p, q);
         cplx<T> v = hb;
         if (m.has_r && p != q) {
@@ -116,7 +117,7 @@ __global__ void __launch_bounds__(256) gauge_kernel(DevModel m, const double* __
     // curvature diagonal: one warp per (q, n), lanes over the summed band m
     const int lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
     for (int t = warp; t < 3 * N; t += nw) {
-        const int q = t / N, n = t % N;
+        const int q = byN.div(t), n = t - q * N;
         const int a = q < 2 ? 0 : 1, b = q == 0 ? 1 : 2;   // (x,y), (x,z), (y,z)
         cplx<T> o = OD[((size_t)k * 3 + q) * N + n];
         if (m.do_gauge) {

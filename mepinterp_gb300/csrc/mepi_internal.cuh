@@ -29,6 +29,17 @@ constexpr int kMaxN = 64;                                // largest n_wf support
 
 template <typename T> struct cplx { T re, im; };
 
+// Division by a divisor fixed for the kernel (a band count N or N^2) by one
+// multiply-high: q = umulhi(e, m), m = floor((2^32 - 1) / d) + 1 >= 2^32 / d,
+// which is exact for every e with e d < 2^32 (the element indices here are
+// below 6 N^2 with N <= 64).
+struct FastDiv {
+    uint32_t m, d;
+    __host__ __device__ explicit FastDiv(int d_) : m(0xFFFFFFFFu / (uint32_t)d_ + 1u), d((uint32_t)d_) {}
+    __device__ __forceinline__ int div(int e) const { return (int)__umulhi((uint32_t)e, m); }
+    __device__ __forceinline__ int mod(int e) const { return e - div(e) * (int)d; }
+};
+
 template <typename T> __host__ __device__ __forceinline__ cplx<T> mk(T r, T i) { cplx<T> c; c.re = r; c.im = i; return c; }
 template <typename T> __host__ __device__ __forceinline__ cplx<T> operator+(cplx<T> a, cplx<T> b) { return mk(a.re + b.re, a.im + b.im); }
 template <typename T> __host__ __device__ __forceinline__ cplx<T> operator-(cplx<T> a, cplx<T> b) { return mk(a.re - b.re, a.im - b.im); }

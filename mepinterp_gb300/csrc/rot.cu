@@ -25,8 +25,9 @@ namespace {
 template <typename T>
 __device__ __forceinline__ void load_hermitian(const cplx<T>* __restrict__ Wb, cplx<T>* Xs, int N, int ld, int tid,
                                                int nt) {
+    const FastDiv byN(N);
     for (int e = tid; e < N * N; e += nt) {
-        const int i = e / N, c = e % N;
+        const int i = byN.div(e), c = e - i * N;
         if (i > c) continue;
         const cplx<T> x = Wb[e];
         Xs[i * ld + c] = x;
@@ -52,6 +53,7 @@ __global__ void __launch_bounds__(256) rot_kernel(DevModel m, const cplx<T>* __r
     const cplx<T>* Wk = W + (size_t)k * nbW * NN;
     const int nmat = m.has_r ? 6 : 3;
     cplx<T>* HAk = HA + (size_t)k * 6 * NN;
+    const FastDiv byN(N);
 
     if (!m.do_gauge) {
         for (int j = 0; j < nmat; ++j)
@@ -88,7 +90,7 @@ __global__ void __launch_bounds__(256) rot_kernel(DevModel m, const cplx<T>* __r
                 __syncthreads();
                 cgemm_dot2<true>(Np, ld, Us, Ts, Tl, Xs, nullptr, true, tid, nt);
                 __syncthreads();
-                for (int e = tid; e < NN; e += nt) HAk[(size_t)j * NN + e] = Xs[(e / N) * ld + e % N];
+                for (int e = tid; e < NN; e += nt) HAk[(size_t)j * NN + e] = Xs[byN.div(e) * ld + byN.mod(e)];
                 continue;
             }
         }
@@ -96,7 +98,7 @@ __global__ void __launch_bounds__(256) rot_kernel(DevModel m, const cplx<T>* __r
         __syncthreads();
         smem_cgemm_herm<T>(Np, ld, Us, Ts, Xs, tid, nt);            // Y = U^dag T (Hermitian, into Xs)
         __syncthreads();
-        for (int e = tid; e < NN; e += nt) HAk[(size_t)j * NN + e] = Xs[(e / N) * ld + e % N];
+        for (int e = tid; e < NN; e += nt) HAk[(size_t)j * NN + e] = Xs[byN.div(e) * ld + byN.mod(e)];
     }
     if (!m.has_r) return;
     // blocks 7..9 (Omega_q): diagonal of U^dag Omega_q U only
