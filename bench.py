@@ -31,6 +31,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
@@ -107,7 +108,7 @@ class ClockSampler:
 
     def __init__(self):
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", "clocks_bench.csv")
+        self.path = os.path.join(tempfile.gettempdir(), f"mepi_bench_clocks_{os.getpid()}.csv")
 
     def start(self):
         try:

@@ -23,7 +23,7 @@ this module spends the k-points where they matter instead:
    acc = coarse - coarse(refined cells) + fine(refined cells) / s^3.
 
 Uniform refinement by the plain FP64 method on the full (s n)^3 mesh stays the
-fallback and is the judge of the result's error (:func:`uniform`).
+fallback, and the result's error is measured against it (:func:`uniform`).
 """
 from __future__ import annotations
 
