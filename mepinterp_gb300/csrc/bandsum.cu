@@ -98,10 +98,7 @@ __global__ void __launch_bounds__(256) bandsum_kernel(DevModel md, JobDev jb, in
     T* lcv = icv + 9 * kMaxN;                                     // [9][kMaxN] Niu LC
     T* Cs = lcv + 9 * kMaxN;                                      // [kMaxN]
     T* Dt = Cs + kMaxN;                                           // [N][N] E_a - E_b (difference formed in FP64)
-    T* Iv = Dt + (use_tab ? NN : 0);                              // [N][N] 1 / (E_a - E_b), 0 on the diagonal
-    // [warp][3][N] V(c, m, n0) / (E0 - Em), aligned for cplx<T>
-    cplx<T>* Wsc = reinterpret_cast<cplx<T>*>((reinterpret_cast<uintptr_t>(Iv + (use_tab ? NN : 0)) + 15) &
-                                              ~uintptr_t(15));
+    T* Iv = Dt + NN;                                              // [N][N] 1 / (E_a - E_b), 0 on the diagonal
     const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nwarps = nt >> 5;
     const AccLayout L{nE, nval, jb.nW};
     double* P = partials + (size_t)blockIdx.x * L.size();
@@ -138,15 +135,6 @@ __global__ void __launch_bounds__(256) bandsum_kernel(DevModel md, JobDev jb, in
 
         for (int n0 = warp; n0 < N; n0 += nwarps) {
             const bool niu = (n0 < nval) && jb.do_mep;
-            // the IC operand of this n0, shared by every lane: W_c(m) = V_c(m, n0) / (E0 - Em)
-            cplx<T>* Wn = Wsc + (size_t)warp * 3 * N;
-            __syncwarp();
-            for (int m = lane; m < N; m += 32) {
-                const T b = iE(n0, m);   // 0 for m = n0
-#pragma unroll
-                for (int c = 0; c < 3; ++c) Wn[c * N + m] = b * V(c, m, n0);
-            }
-            __syncwarp();
             // per-band curvature: FP64 in the FP64 form, double-FP32 (TwoSum) in
             // the FP32 form, so that the pair terms of two occupied bands still
             // cancel to well below the FP32 rounding of one term
@@ -215,15 +203,16 @@ __global__ void __launch_bounds__(256) bandsum_kernel(DevModel md, JobDev jb, in
                     const T a2 = d0n * d0n;
                     for (int m = 0; m < N; ++m) {
                         if (m == n0) continue;
-                        cplx<T> vnm[3], wm[3], x[3];
+                        cplx<T> vnm[3], vmo[3], x[3];
 #pragma unroll
-                        for (int c = 0; c < 3; ++c) { vnm[c] = V(c, n, m); wm[c] = Wn[c * N + m]; }
-                        cross3(vnm, wm, x);   // (V(n,m) x V(m,n0)) / (E0 - Em)
+                        for (int c = 0; c < 3; ++c) { vnm[c] = V(c, n, m); vmo[c] = V(c, m, n0); }
+                        cross3(vnm, vmo, x);
+                        const T b = iE(n0, m);
 #pragma unroll
-                        for (int c = 0; c < 3; ++c) g[c] = g[c] + x[c];
+                        for (int c = 0; c < 3; ++c) g[c] = g[c] + b * x[c];
                         if (niu && fabs(a2 * dE(n0, m)) > ttol) {
 #pragma unroll
-                            for (int c = 0; c < 3; ++c) gv[c] = gv[c] + x[c];
+                            for (int c = 0; c < 3; ++c) gv[c] = gv[c] + b * x[c];
                         }
                     }
                     const T ainv = i0n * i0n;
@@ -514,9 +503,7 @@ size_t bandsum_smem(int N, bool tables) {
     size_t b = 3 * (size_t)N * (N + 1) * sizeof(cplx<T>);
     b += (9 * (size_t)N + kMaxN) * sizeof(double);
     b += (18 * (size_t)N + 18 * kMaxN + kMaxN + (tables ? 2 * (size_t)N * N : 0)) * sizeof(T);
-    b = (b + 15) & ~(size_t)15;
-    b += 16 + 8 * 3 * (size_t)N * sizeof(cplx<T>);   // per-warp IC operand (8 warps), aligned
-    return b;
+    return (b + 15) & ~(size_t)15;
 }
 
 template <typename T>

@@ -174,11 +174,10 @@ __global__ void __launch_bounds__(128) sep_w_kernel(DevModel m, KRange kr, const
     const int NN = m.N * m.N, PT = blockDim.x, t = threadIdx.x;
     load_items<TG, KI>(h, kr, nbz, rz0, (size_t)nbz * NB * NN, m.has_tau ? m.tau : nullptr, m.N, qx0, nqx);
     // every block is Hermitian and its consumers read the upper triangle: the
-    // CTAs of one item group (blockIdx.y) walk the N (N + 1) / 2 elements n <= m
-    // in tiles of PT, gridDim.y tiles apart (more CTAs keep more of the output
-    // stores in flight; fewer form the item header fewer times)
-    const int NU = m.N * (m.N + 1) / 2;
-    for (int u = blockIdx.y * PT + t; u < NU; u += PT * gridDim.y) {
+    // CTA's threads take the elements n <= m of its pair tile (blockIdx.y)
+    const int u = blockIdx.y * PT + t;
+    if (u >= m.N * (m.N + 1) / 2) return;
+    {
         int n, mm;
         upper_pair(u, m.N, n, mm);
         const int pair = n * m.N + mm;
