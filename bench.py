@@ -38,6 +38,16 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "k-points/s for AHE+MEP, nWf=32"
+
+# measured DRAM bytes per k-point by (workload, form, stage): ncu captures of
+# the tb32 model on a 32^3 mesh, one 32,768-k launch per kernel
+NCU_DRAM_BYTES_PER_K = {
+    ("tb32_r3_k128", "mixed", "rot"): (2.08e9 + 1.60e9) / 32768,
+    ("tb32_r3_k128", "mixed", "eig"): (0.339e9 + 0.230e9) / 32768,
+    ("tb32_r3_k128", "mixed", "refine"): (0.609e9 + 0.238e9) / 32768,
+    ("tb32_r3_k128", "mixed", "gauge"): (1.64e9 + 0.779e9) / 32768,
+    ("tb32_r3_k128", "mixed", "fth"): (0.0895e9 + 0.231e9) / 32768,
+}
 UNIT = "k-points/s"
 
 
@@ -333,7 +343,14 @@ def run_gpu(args, rank, world):
         pipe, pipe_peak = ("fp32", 68.0) if mixed and dom != "fth" else ("fp64", 1.19)
         roofline["cuda_core"] = {"pipe": pipe, "peak_tflops": pipe_peak, "frac": achieved / pipe_peak,
                                  "peak_source": "FMA-chain probe on a GB300 of this pool"}
-    roofline.update({"traffic": None, "flops_per_launch": flops_per_launch, "bytes_per_launch": bytes_per_launch,
+    # DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) per k-point of the
+    # dominant kernel, from the ncu capture of this model on a 32^3 mesh (one
+    # 32,768-k launch per kernel, buffers far above L2), scaled to this run's launch
+    per_k = NCU_DRAM_BYTES_PER_K.get((args.workload, args.precision, dom))
+    traffic = per_k * nk * args.steps / n_launch if per_k else None
+    roofline.update({"traffic": traffic, "traffic_source": "ncu --set full, 32^3 case of this model, scaled by k per launch"
+                     if traffic else None,
+                     "flops_per_launch": flops_per_launch, "bytes_per_launch": bytes_per_launch,
                      "avg_launch_ms": avg_launch_s * 1e3,
                      "stage_ms_per_step": {k: v / args.steps for k, v in stage_ms.items()}})
 
