@@ -85,7 +85,6 @@ __global__ void __launch_bounds__(256) bandsum_kernel(DevModel md, JobDev jb, in
                                                       int use_tab) {
     extern __shared__ unsigned char smem_raw[];
     const int N = md.N, NN = N * N, ld = N + 1;
-    const FastDiv byN(N);
     const int nval = jb.nval, nE = jb.nE;
     cplx<T>* Vs = reinterpret_cast<cplx<T>*>(smem_raw);          // [3][N][ld]
     double* curv = reinterpret_cast<double*>(Vs + 3 * N * ld);    // [9][N] AHC curvature per band: FP64, or
@@ -108,8 +107,8 @@ __global__ void __launch_bounds__(256) bandsum_kernel(DevModel md, JobDev jb, in
         if (skip && skip[k]) continue;
         __syncthreads();
         for (int e = tid; e < 3 * NN; e += nt) {
-            const int row = byN.div(e), m = e - row * N;   // row = a * N + n
-            Vs[row * ld + m] = Vg[(size_t)k * 3 * NN + e];
+            int a = e / NN, r = e % NN, n = r / N, m = r % N;
+            Vs[(a * N + n) * ld + m] = Vg[(size_t)k * 3 * NN + e];
         }
         for (int n = tid; n < N; n += nt) {
             Es[n] = Eg[(size_t)k * N + n];
@@ -118,7 +117,7 @@ __global__ void __launch_bounds__(256) bandsum_kernel(DevModel md, JobDev jb, in
         __syncthreads();
         if (use_tab) {
             for (int e = tid; e < NN; e += nt) {
-                const int a = byN.div(e), b = e - a * N;
+                const int a = e / N, b = e % N;
                 const T d = (T)(Es[a] - Es[b]);
                 Dt[e] = d;
                 Iv[e] = (a == b) ? (T)0 : (T)1 / d;
@@ -354,7 +353,6 @@ __global__ void __launch_bounds__(256) opt_hall_kernel(DevModel md, JobDev jb, i
     constexpr int ET = f32 ? 64 : 8;   // Fermi energies per occupation tile
     extern __shared__ unsigned char smem_raw[];
     const int N = md.N, NN = N * N, ld = N + 1;
-    const FastDiv byN(N);
     const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nwarps = nt >> 5;
     cplx<T>* Vs = reinterpret_cast<cplx<T>*>(smem_raw);   // [3][N][ld]
     T* Ys = reinterpret_cast<T*>(Vs + 3 * N * ld);         // [N][36] per-band sums (leading part)
@@ -370,14 +368,14 @@ __global__ void __launch_bounds__(256) opt_hall_kernel(DevModel md, JobDev jb, i
         if (skip && skip[k]) continue;
         __syncthreads();
         for (int e = tid; e < 3 * NN; e += nt) {
-            const int row = byN.div(e);
-            Vs[row * ld + (e - row * N)] = Vg[(size_t)k * 3 * NN + e];
+            const int a = e / NN, r = e % NN;
+            Vs[(a * N + r / N) * ld + r % N] = Vg[(size_t)k * 3 * NN + e];
         }
         for (int n = tid; n < N; n += nt) Es[n] = Eg[(size_t)k * N + n];
         if constexpr (f32) {
             __syncthreads();
             for (int e = tid; e < NN; e += nt) {
-                const double d = Es[byN.div(e)] - Es[byN.mod(e)];
+                const double d = Es[e / N] - Es[e % N];
                 const T hi = (T)d;
                 dEh[e] = hi;
                 dEl[e] = (T)(d - (double)hi);
