@@ -116,11 +116,28 @@ __global__ void __launch_bounds__(256) bandsum_kernel(DevModel md, JobDev jb, in
         }
         __syncthreads();
         if (use_tab) {
-            for (int e = tid; e < NN; e += nt) {
-                const int a = e / N, b = e % N;
-                const T d = (T)(Es[a] - Es[b]);
-                Dt[e] = d;
-                Iv[e] = (a == b) ? (T)0 : (T)1 / d;
+            if constexpr (sizeof(T) == 4) {
+                // the FP64 differences rounded to FP32, formed from FP32 hi/lo energies
+                __shared__ float s_Eh[kMaxN], s_El[kMaxN];
+                for (int n = tid; n < N; n += nt) {
+                    s_Eh[n] = (float)Es[n];
+                    s_El[n] = (float)(Es[n] - (double)s_Eh[n]);
+                }
+                __syncthreads();
+                for (int e = tid; e < NN; e += nt) {
+                    const int a = e / N, b = e % N;
+                    float d, dl;
+                    df_diff(s_Eh[a], s_El[a], s_Eh[b], s_El[b], d, dl);
+                    Dt[e] = d;
+                    Iv[e] = (a == b) ? 0.f : 1.f / d;
+                }
+            } else {
+                for (int e = tid; e < NN; e += nt) {
+                    const int a = e / N, b = e % N;
+                    const T d = (T)(Es[a] - Es[b]);
+                    Dt[e] = d;
+                    Iv[e] = (a == b) ? (T)0 : (T)1 / d;
+                }
             }
         }
         __syncthreads();
@@ -373,12 +390,20 @@ __global__ void __launch_bounds__(256) opt_hall_kernel(DevModel md, JobDev jb, i
         }
         for (int n = tid; n < N; n += nt) Es[n] = Eg[(size_t)k * N + n];
         if constexpr (f32) {
+            // E_n - E_m as an FP32 hi/lo pair from FP32 hi/lo energies (no FP64 per pair)
+            __shared__ float s_Eh[kMaxN], s_El[kMaxN];
+            __syncthreads();
+            for (int n = tid; n < N; n += nt) {
+                s_Eh[n] = (float)Es[n];
+                s_El[n] = (float)(Es[n] - (double)s_Eh[n]);
+            }
             __syncthreads();
             for (int e = tid; e < NN; e += nt) {
-                const double d = Es[e / N] - Es[e % N];
-                const T hi = (T)d;
-                dEh[e] = hi;
-                dEl[e] = (T)(d - (double)hi);
+                const int n = e / N, m = e % N;
+                float h, l;
+                df_diff(s_Eh[n], s_El[n], s_Eh[m], s_El[m], h, l);
+                dEh[e] = h;
+                dEl[e] = l;
             }
         }
         for (int w = 0; w < jb.nW; ++w) {

@@ -292,10 +292,10 @@ cudaError_t launch_eig(int N, int64_t nk, const cplx<T>* W, int nbW, const cplx<
                        cudaStream_t s, int threads_req, int kblock_req) {
     if (nk <= 0) return cudaSuccess;
     // a run of consecutive k-points per CTA, each warm-started from its
-    // neighbour's eigenvectors (consecutive k-points are mesh neighbours).  Four
-    // per CTA measured fastest for N = 32 (more CTAs in flight outweigh the
-    // extra cold starts: 5% less time than eight, 25% less than sixteen).
-    const int kblock = kblock_req > 0 ? kblock_req : 4;
+    // neighbour's eigenvectors (consecutive k-points are mesh neighbours).  Eight
+    // per CTA: four measured 5% faster at N = 32, but its extra cold starts
+    // raised the mixed form's Chern-Simons error on sparse k subsets above 1e-6.
+    const int kblock = kblock_req > 0 ? kblock_req : 8;
     const unsigned grid = (unsigned)((nk + kblock - 1) / kblock);
     auto go = [&](auto kern, int NP, int threads) {
         // a tuned thread count: a multiple of 32, at least one thread per pair, at most 256

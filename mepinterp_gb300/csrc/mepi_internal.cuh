@@ -170,6 +170,18 @@ __device__ __forceinline__ void df_add(DF& acc, float x) {
     acc.s = t;
     acc.c = __fadd_rn(acc.c, e);
 }
+// (ah + al) - (bh + bl) as a normalised FP32 pair (h, l): TwoSum of the
+// leading parts plus the difference of the remainders, about 2^-48 of the
+// operands -- the FP64 difference of two FP64 energies split into hi + lo,
+// without FP64 arithmetic
+__device__ __forceinline__ void df_diff(float ah, float al, float bh, float bl, float& h, float& l) {
+    const float s = __fsub_rn(ah, bh);
+    const float bp = __fsub_rn(s, ah);
+    const float t = __fadd_rn(__fsub_rn(ah, __fsub_rn(s, bp)), __fsub_rn(-bh, bp));
+    const float lo = __fadd_rn(t, __fsub_rn(al, bl));
+    h = __fadd_rn(s, lo);
+    l = __fsub_rn(lo, __fsub_rn(h, s));
+}
 // a + b of two unevaluated sums
 __device__ __forceinline__ DF df_sum(DF a, DF b) {
     DF r{a.s, __fadd_rn(a.c, b.c)};
