@@ -2,7 +2,8 @@
 // (src/matrix_math.f90:192-226: jobz='V', uplo='U', eigenvalues ascending,
 // eigenvectors in the columns of U).
 //
-// A CTA diagonalises a run of consecutive k-points (adjacent along kx): the
+// A CTA diagonalises a run of consecutive k-points of the run's order (mesh
+// neighbours along kz within a (qx, qy) column for the separable sums): the
 // first from the identity, each next one warm-started from its neighbour's
 // eigenvectors V as V^dag H V, which typically needs a few sweeps instead of
 // six or seven.  The matrix and the eigenvector accumulator live in shared
