@@ -118,3 +118,32 @@ def test_no_gpu_fails_loudly(lib):
     with pytest.raises(api.MepiError) as e:
         api.Context(model)
     assert e.value.status == api.ERR_CUDA
+
+
+def test_null_contexts_and_bad_counts_are_rejected(lib):
+    """The entry points added beside mepi_run answer NULL contexts and bad
+    counts with MEPI_ERR_ARG before any device work."""
+    P = C.c_void_p
+    lib.mepi_trim.argtypes = [P]
+    lib.mepi_set_mem_limit.argtypes = [P, C.c_uint64]
+    lib.mepi_run_batch.argtypes = [C.c_int32, P, P, P, P]
+    assert lib.mepi_trim(None) == api.ERR_ARG
+    assert lib.mepi_set_mem_limit(None, 1 << 20) == api.ERR_ARG
+    assert lib.mepi_run_batch(-1, None, None, None, None) == api.ERR_ARG
+    assert lib.mepi_run_batch(0, None, None, None, None) == api.OK
+    assert lib.mepi_run_batch(2, None, None, None, None) == api.ERR_ARG
+
+
+def test_mlp_create_checks_shape_then_device(lib):
+    """mepi_mlp_create rejects bad shapes (n_in 1..64, width 128, depth 1..8)
+    with MEPI_ERR_ARG and, without a CUDA device, valid ones with
+    MEPI_ERR_CUDA: the network has no CPU fallback."""
+    import torch
+    f = lib.mepi_mlp_create
+    f.argtypes = [C.POINTER(C.c_void_p), C.c_int32, C.c_int32, C.c_int32, C.c_uint64]
+    h = C.c_void_p()
+    for n_in, width, depth in ((0, 128, 4), (65, 128, 4), (31, 64, 4), (31, 128, 0), (31, 128, 9)):
+        assert f(C.byref(h), n_in, width, depth, 0) == api.ERR_ARG
+    assert f(None, 31, 128, 4, 0) == api.ERR_ARG
+    if not torch.cuda.is_available():
+        assert f(C.byref(h), 31, 128, 4, 0) == api.ERR_CUDA
