@@ -94,3 +94,19 @@ def test_learned_proposal_beats_the_method_without_it(gpu_lib):
     assert max(mlp) < 0.7 * none, (mlp, none)
     assert max(mlp) < min(rand), (mlp, rand)
     assert np.mean(mlp) < omega, (mlp, omega)
+
+
+def test_batch_workload_matches_its_recipe():
+    """The batched form's 64 models: nWf even in 4..64, R shells 1..3, meshes
+    from {32, 48, 64, 96}, 201 Fermi energies over [-1, 1] eV at 290.1 K."""
+    from mepinterp_gb300.generator import batch_workload
+    work = batch_workload(64)
+    assert len(work) == 64
+    for m, j in work:
+        assert m.n_wf % 2 == 0 and 4 <= m.n_wf <= 64
+        assert m.n_R in (27, 125, 343)
+        assert j["mp_grid"][0] in (32, 48, 64, 96) and len(set(j["mp_grid"])) == 1
+        assert len(j["ef_lst"]) == 201 and abs(j["ef_lst"][-1] * AU_TO_EV - 1.0) < 1e-12
+        assert j["T_kelvin"] == 290.1 and j["valence_bands"] == m.n_wf // 2
+    again = batch_workload(64)
+    assert all(np.array_equal(a[0].H, b[0].H) for a, b in zip(work[:3], again[:3]))   # seeded
