@@ -3,6 +3,9 @@
 * FeMn AHC goldens (config/FeMn_TB/delta*/ahc_tens.npy, ahcVELO_sol*.npy)
 * the k-mesh Gaussian integral of tests/test_kSpace.f90:140-273
 * U^dag H U = diag(E) of tests/test_matrix_math.f90:274-336
+* the Levi-Civita, cross-product and commutator checks of
+  tests/test_matrix_math.f90:79-133,417-498 and the reciprocal lattice of
+  tests/test_kSpace.f90:60-130
 * agreement of the two independent restatements (numpy and C)
 * invariances the reference's algorithm has (per-band phases, k partition,
   constant energy shift)
@@ -200,3 +203,43 @@ def test_energy_shift():
     a, b = O.run(m, job), O.run(m2, job2)
     for k in KEYS:
         assert rel(b[k], a[k]) < 1e-9, k
+
+
+def test_levi_civita_and_cross_product():
+    """tests/test_matrix_math.f90:79-133: the Levi-Civita symbol and the cross
+    product built on it (the form the MEP sums use)."""
+    e = O.levi_civita()
+    assert e[0, 1, 2] == 1 and e[2, 1, 0] == -1 and np.count_nonzero(e) == 6
+    assert np.allclose(e, -np.swapaxes(e, 0, 1))
+    rng = np.random.default_rng(2)
+    a, b = rng.normal(size=3), rng.normal(size=3)
+    assert np.allclose(np.einsum("ijk,j,k->i", e, a, b), np.cross(a, b))
+    assert np.allclose(np.einsum("ijk,j,k->i", e, [1, 0, 0], [0, 1, 0]), [0, 0, 1])
+
+
+def test_reciprocal_lattice_of_a_diagonal_cell():
+    """tests/test_kSpace.f90:60-130: b_i = 2 pi / a_i for a diagonal cell and
+    a_i . b_j = 2 pi delta_ij in general."""
+    a = np.diag([3.0, 4.5, 7.25])
+    b, vol = O.recip_latt(a)
+    assert np.isclose(vol, 3.0 * 4.5 * 7.25)
+    assert np.allclose(b, np.diag(2 * np.pi / np.diag(a)))
+    rng = np.random.default_rng(3)
+    a = np.eye(3) * 5.0 + rng.normal(scale=0.5, size=(3, 3))
+    b, _ = O.recip_latt(a)
+    assert np.allclose(a.T @ b, 2 * np.pi * np.eye(3))
+
+
+def test_commutator_identities():
+    """tests/test_matrix_math.f90:417-498: [A, B] = -[B, A], the Jacobi identity,
+    and the commutator of two Hermitian matrices is anti-Hermitian."""
+    rng = np.random.default_rng(4)
+    def herm(n):
+        x = rng.normal(size=(n, n)) + 1j * rng.normal(size=(n, n))
+        return x + x.conj().T
+    A, B, C = herm(12), herm(12), herm(12)
+    assert np.allclose(O._comm(A, B), -O._comm(B, A))
+    jac = O._comm(A, O._comm(B, C)) + O._comm(B, O._comm(C, A)) + O._comm(C, O._comm(A, B))
+    assert np.abs(jac).max() < 1e-10 * np.abs(A).max() ** 3
+    K = O._comm(A, B)
+    assert np.allclose(K, -K.conj().T)
