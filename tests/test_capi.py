@@ -147,3 +147,60 @@ def test_mlp_create_checks_shape_then_device(lib):
     assert f(None, 31, 128, 4, 0) == api.ERR_ARG
     if not torch.cuda.is_available():
         assert f(C.byref(h), 31, 128, 4, 0) == api.ERR_CUDA
+
+
+C_CALLER = r"""
+#include <stdio.h>
+#include <string.h>
+#include "mepi.h"
+/* A plain C caller of the k-loop: one-band-pair toy model, a 2^3 mesh. */
+int main(void) {
+    const double R[3 * 3] = {0, 0, 0, 1, 0, 0, -1, 0, 0};
+    double H[2 * 2 * 2 * 3];   /* complex H(2,2,3), column-major */
+    memset(H, 0, sizeof H);
+    H[0] = -0.1; H[6] = 0.1;                  /* R = 0: diag(-0.1, 0.1) */
+    H[8 + 2] = 0.05; H[16 + 4] = 0.05;        /* R = +x: H(2,1); R = -x: H(1,2) = conj */
+    mepi_model m;
+    memset(&m, 0, sizeof m);
+    m.n_wf = 2; m.n_R = 3; m.R_frac = R; m.H = H;
+    m.a_latt[0] = m.a_latt[4] = m.a_latt[8] = 5.0;
+    m.do_gauge_trafo = 1; m.kubo_tol = 1e-5;
+    mepi_ctx *ctx = NULL;
+    int rc = mepi_create(&ctx, &m);
+    if (rc == MEPI_OK) {
+        const double ef = 0.0;
+        double ahc[9], ne;
+        mepi_job j;
+        memset(&j, 0, sizeof j);
+        j.mp_grid[0] = j.mp_grid[1] = j.mp_grid[2] = 2; j.k_stride = 1; j.k_count = -1;
+        j.n_eF = 1; j.ef_lst = &ef; j.valence_bands = 1; j.outputs = MEPI_OUT_AHC; j.degen_gap = -1;
+        mepi_acc a;
+        memset(&a, 0, sizeof a);
+        a.ahc = ahc; a.Ne_sum = &ne;
+        rc = mepi_run(ctx, &j, &a);
+        if (rc == MEPI_OK) printf("n_k %lld Ne %.6f\n", (long long)a.n_k_done, ne);
+        mepi_destroy(ctx);
+    }
+    printf("status %d %s\n", rc, mepi_strerror(rc));
+    return 0;
+}
+"""
+
+
+def test_plain_c_caller_links_and_runs(lib, tmp_path):
+    """The C ABI used from plain C (as a Fortran shim or a C++ driver would):
+    the program compiles against include/mepi.h, links libmepi_gb300.so and
+    runs; without a GPU mepi_create answers MEPI_ERR_CUDA, with one the 2^3
+    mesh of the toy model is summed (8 k-points, one electron each)."""
+    import torch
+    c = tmp_path / "caller.c"
+    c.write_text(C_CALLER)
+    exe = tmp_path / "caller"
+    libdir = os.path.dirname(build.LIB)
+    subprocess.check_call(["gcc", "-I", os.path.join(ROOT, "include"), str(c), "-L", libdir, "-lmepi_gb300",
+                           f"-Wl,-rpath,{libdir}", "-o", str(exe)])
+    out = subprocess.check_output([str(exe)]).decode()
+    if torch.cuda.is_available():
+        assert "status 0" in out and "n_k 8 Ne 8.000000" in out, out
+    else:
+        assert f"status {api.ERR_CUDA}" in out, out
