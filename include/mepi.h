@@ -245,8 +245,12 @@ int mepi_run_batch(int32_t n, mepi_ctx *const *ctxs, const mepi_job *jobs, mepi_
  * 37*n_eF + 27*valence_bands > 3449 are rejected with MEPI_ERR_SCRATCH.  All
  * calls share that array, so calls whose work overlaps on the GPU (on
  * different streams, or from several host threads) race; serialise them.  The
- * first call on each device looks up the array's device address; make that
- * first call before capturing any stream. */
+ * first call on each device (and the first after that device's context is
+ * replaced, e.g. by cudaDeviceReset) looks up the array's device address; make
+ * that first call before capturing any stream.  Only the outputs bits
+ * MEPI_OUT_AHC, MEPI_OUT_MEP_NIU and MEPI_OUT_KUBO_MEP are honoured; any other
+ * bit is rejected with MEPI_ERR_ARG, as are a non-finite T_kelvin or kubo_tol.
+ * ef_lst lives in device memory and is not validated. */
 int mepi_bandsum_noalloc(int32_t n_wf, int64_t n_k, const double *en_k, const double *V, const double *csv,
                          int32_t n_eF, const double *ef_lst, double T_kelvin, int32_t valence_bands,
                          uint32_t outputs, double kubo_tol, double *sums, void *stream);

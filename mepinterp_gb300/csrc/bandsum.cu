@@ -21,6 +21,7 @@
 // Fermi energy.  A CTA owns one FP64 accumulator slice for its whole k stripe
 // (k = blockIdx.x, blockIdx.x + gridDim.x, ...), so the final reduction over
 // slices runs in a fixed order and the result is deterministic.
+#include <cmath>
 #include <mutex>
 
 #include "../../include/mepi.h"
@@ -660,23 +661,58 @@ constexpr int kMaxDevices = 64;
 static __device__ __align__(256) double g_noalloc_partials[kNoAllocDoubles];
 
 std::mutex g_noalloc_mu;
-double* g_noalloc_ptr[kMaxDevices] = {};
+struct NoAllocSlot {
+    unsigned long long ctx_id = 0;   // CUDA context the address belongs to
+    double* ptr = nullptr;
+};
+NoAllocSlot g_noalloc_slot[kMaxDevices];
 
-// Device address of the scratch array on the current device, looked up once
-// per device (the host-side symbol is only a stand-in, not a device address).
+// Unique id of the calling thread's current CUDA context (cuCtxGetId through
+// the runtime's driver entry point), 0 if it cannot be had.
+unsigned long long current_ctx_id() {
+    using GetCurrent = int (*)(void**);
+    using GetId = int (*)(void*, unsigned long long*);
+    static GetCurrent get_current = nullptr;
+    static GetId get_id = nullptr;
+    static bool looked_up = false;
+    if (!looked_up) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = reinterpret_cast<GetCurrent>(p);
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<GetId>(p);
+        looked_up = true;
+    }
+    void* ctx = nullptr;
+    unsigned long long id = 0;
+    if (!get_current || !get_id || get_current(&ctx) != 0 || !ctx || get_id(ctx, &id) != 0) return 0;
+    return id;
+}
+
+// Device address of the scratch array on the current device.  The host-side
+// symbol is only a stand-in, not a device address, so the address is looked
+// up with cudaGetSymbolAddress once per device, with that device current, and
+// looked up again when the device's context changes (after a cudaDeviceReset
+// the module is loaded anew and the array may sit elsewhere).
 cudaError_t noalloc_scratch(double** out) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
     std::lock_guard<std::mutex> lock(g_noalloc_mu);
-    if (!g_noalloc_ptr[dev]) {
+    NoAllocSlot& slot = g_noalloc_slot[dev];
+    const unsigned long long id = current_ctx_id();   // 0 before the context exists
+    if (!slot.ptr || id == 0 || id != slot.ctx_id) {
         void* p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_noalloc_partials);
+        e = cudaGetSymbolAddress(&p, g_noalloc_partials);   // initialises the context if needed
         if (e != cudaSuccess) return e;
-        g_noalloc_ptr[dev] = static_cast<double*>(p);
+        slot.ptr = static_cast<double*>(p);
+        slot.ctx_id = current_ctx_id();
     }
-    *out = g_noalloc_ptr[dev];
+    *out = slot.ptr;
     return cudaSuccess;
 }
 }  // namespace
@@ -691,9 +727,12 @@ extern "C" int mepi_bandsum_noalloc(int32_t n_wf, int64_t n_k, const double* en_
     if (n_wf <= 0 || n_wf > kMaxN || n_k < 0 || n_eF <= 0 || valence_bands < 0 || valence_bands > n_wf)
         return MEPI_ERR_ARG;
     if (!ef_lst || !sums || (n_k > 0 && (!en_k || !V))) return MEPI_ERR_ARG;
-    if (!(kubo_tol >= 0.0) || !(T_kelvin == T_kelvin)) return MEPI_ERR_ARG;
+    if (!(kubo_tol >= 0.0) || !std::isfinite(T_kelvin) || !std::isfinite(kubo_tol)) return MEPI_ERR_ARG;
+    if (outputs & ~(uint32_t)(MEPI_OUT_AHC | MEPI_OUT_MEP_NIU | MEPI_OUT_KUBO_MEP)) return MEPI_ERR_ARG;
+    // bound the slice size in 64-bit arithmetic before any int-sized layout
+    const int64_t slice = 37 * (int64_t)n_eF + 27 * (int64_t)valence_bands;
+    if (slice * kNoAllocCtas > (int64_t)kNoAllocDoubles) return MEPI_ERR_SCRATCH;
     const AccLayout L{n_eF, valence_bands};
-    if ((size_t)kNoAllocCtas * (size_t)L.size() > kNoAllocDoubles) return MEPI_ERR_SCRATCH;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     double* scratch = nullptr;
     if (noalloc_scratch(&scratch) != cudaSuccess) return MEPI_ERR_CUDA;

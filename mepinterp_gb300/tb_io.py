@@ -25,6 +25,7 @@ from __future__ import annotations
 import configparser
 import datetime
 import os
+import warnings
 from typing import Optional
 
 import numpy as np
@@ -64,8 +65,13 @@ def read_hr_file(path: str):
     arr = np.array([[float(x) for x in row[:7]] for row in body[: n_r * n_wf * n_wf]])
     arr = arr.reshape(n_r, n_wf * n_wf, 7)
     R = arr[:, 0, :3].copy()
-    if not np.all(np.abs(arr[:, :, :3] - R[:, None, :]) < 1e-14):
-        raise TBFormatError(f"{path}: unexpected new R_vect inside an R block")
+    # an R vector that changes inside its block: the reference warns, keeps the
+    # block's first R and still stores the element (src/file_io.f90:720-727)
+    bad = np.argwhere(np.any(np.abs(arr[:, :, :3] - R[:, None, :]) >= 1e-14, axis=2))
+    for sc, wf in bad:
+        warnings.warn(f"[read_hr_file]: WARNING unexpected new R_vect={arr[sc, wf, :3].tolist()} "
+                      f"m={int(arr[sc, wf, 3])} n={int(arr[sc, wf, 4])} wf={wf + 1} sc={sc + 1} "
+                      f"expected R_vect={R[sc].tolist()}", RuntimeWarning, stacklevel=2)
     m = arr[:, :, 3].astype(int) - 1
     n = arr[:, :, 4].astype(int) - 1
     re = arr[:, :, 5].copy()

@@ -167,18 +167,23 @@ static void put_comp(int N, zc *X, int stride, int off, const zc *M) {
 }
 
 /* ---------------- FT_R_to_k (src/wann_interp.f90:151-384) ---------------- */
-static void ft_R_to_k(const oracle_model *md, const double kpt[3], ws_t *w) {
-    const int N = md->n_wf, nR = md->n_R;
+static void ft_zero(int N, ws_t *w) {
+    const size_t NN = (size_t)N * N;
+    memset(w->Hk, 0, NN * sizeof(zc));
+    memset(w->Hka, 0, 3 * NN * sizeof(zc));
+    memset(w->Aka, 0, 3 * NN * sizeof(zc));
+    memset(w->Omk, 0, 9 * NN * sizeof(zc));
+}
+
+/* adds the terms of R vectors sc0 <= sc < sc1 into w's Hk, Hka, Aka, Omk */
+static void ft_accum(const oracle_model *md, const double kpt[3], ws_t *w, int sc0, int sc1) {
+    const int N = md->n_wf;
     const size_t NN = (size_t)N * N;
     const zc *H = (const zc *)md->H;
     const zc *r = (const zc *)md->r;
     const double *a = md->a_latt; /* column-major a(i,j) = a[i+3j] */
     const double two_pi = 2.0 * PI_DP;
     const int use_pos = (r != 0);
-    memset(w->Hk, 0, NN * sizeof(zc));
-    memset(w->Hka, 0, 3 * NN * sizeof(zc));
-    memset(w->Aka, 0, 3 * NN * sizeof(zc));
-    memset(w->Omk, 0, 9 * NN * sizeof(zc));
     /* kpt_cart = matmul(recip_latt, kpt) (src/k_space.f90:378-396) */
     double kc[3] = {0, 0, 0};
     if (md->use_cart_velo) {
@@ -192,7 +197,7 @@ static void ft_R_to_k(const oracle_model *md, const double kpt[3], ws_t *w) {
                     (2 * PI_DP * c12[i] / vol) * kpt[2];
     }
     const double *tau = md->wf_centers;
-    for (int sc = 0; sc < nR; ++sc) {
+    for (int sc = sc0; sc < sc1; ++sc) {
         const double *R = md->R_frac + 3 * sc;
         for (int m = 0; m < N; ++m)
             for (int n = 0; n < N; ++n) {
@@ -230,6 +235,11 @@ static void ft_R_to_k(const oracle_model *md, const double kpt[3], ws_t *w) {
                 }
             }
     }
+}
+
+static void ft_R_to_k(const oracle_model *md, const double kpt[3], ws_t *w) {
+    ft_zero(md->n_wf, w);
+    ft_accum(md, kpt, w, 0, md->n_R);
 }
 
 /* ---------------- W -> H gauge (src/wann_interp.f90:465-658) ---------------- */
@@ -331,9 +341,9 @@ static double fd_stat(double e_band, double e_fermi, double T_kelvin) { /* src/s
 }
 
 /* full per-k interpolation (src/wann_interp.f90:56-108) */
-static int interp_k(const oracle_model *md, const double kpt[3], ws_t *w, zc *Abar) {
+/* get_wann_interp after FT_R_to_k: eigensolve, gauge transformation, velocity */
+static int interp_after_ft(const oracle_model *md, ws_t *w, zc *Abar) {
     const int N = w->N;
-    ft_R_to_k(md, kpt, w);
     memcpy(w->U, w->Hk, (size_t)N * N * sizeof(zc));
     if (!g_zheevd) return -2;
     int n = N, lwork = N * N + 2 * N, lrwork = 2 * N * N + 5 * N + 1, liwork = 5 * N + 3, info = 0;
@@ -344,6 +354,11 @@ static int interp_k(const oracle_model *md, const double kpt[3], ws_t *w, zc *Ab
     }
     get_velo(md, w, (md->do_gauge_trafo && md->r) ? Abar : 0);
     return 0;
+}
+
+static int interp_k(const oracle_model *md, const double kpt[3], ws_t *w, zc *Abar) {
+    ft_R_to_k(md, kpt, w);
+    return interp_after_ft(md, w, Abar);
 }
 
 /* band sums for one k, added into the given accumulators */
@@ -596,6 +611,70 @@ int oracle_run(const oracle_model *md, const oracle_job *jb, int64_t k_begin, in
     }
     free(part);
     free(cnt);
+    return err;
+}
+
+/* The same sums with the reference's parallel structure (src/core.f90:165-270
+ * around src/wann_interp.f90:206-241): a serial loop over k; inside each k the
+ * Fourier sum runs over R on all threads, each thread summing a contiguous R
+ * range into private matrices that are then added in thread order (the
+ * reference's OpenMP array reduction); the eigensolve, gauge transformation
+ * and band sums of that k run on one thread. */
+int oracle_run_kserial(const oracle_model *md, const oracle_job *jb, int64_t k_begin, int64_t k_count,
+                       int64_t k_stride, oracle_out *out, int nthreads) {
+    const int N = md->n_wf, nE = jb->n_eF, nv = jb->valence_bands, nR = md->n_R;
+    if (N <= 0 || nR <= 0 || nE <= 0 || nv < 0 || nv > N) return -1;
+    if (!g_zheevd) return -2;
+#ifdef _OPENMP
+    if (nthreads <= 0) nthreads = omp_get_max_threads();
+#else
+    nthreads = 1;
+#endif
+    const size_t NN = (size_t)N * N;
+    const int omega = jb->do_ahc && jb->n_hw > 0 && jb->hw_lst && out->velo_ahc && out->kubo_ohc;
+    oracle_job jl = *jb;
+    if (!omega) jl.n_hw = 0;
+    ws_t w = ws_alloc(N, nE);
+    ws_t *tw = calloc(nthreads, sizeof(ws_t));
+    zc *Abar = md->r ? calloc(3 * NN, sizeof(zc)) : 0;
+    if (!tw) return -1;
+    for (int t = 0; t < nthreads; ++t) tw[t] = ws_alloc(N, 1);
+    int err = 0;
+    for (int64_t s = 0; s < k_count && !err; ++s) {
+        double k[3];
+        rel_kpt(jb->mp_grid, k_begin + s * k_stride, k);
+#pragma omp parallel num_threads(nthreads)
+        {
+            int t = 0;
+#ifdef _OPENMP
+            t = omp_get_thread_num();
+#endif
+            ft_zero(N, &tw[t]);
+            ft_accum(md, k, &tw[t], (int)((int64_t)nR * t / nthreads), (int)((int64_t)nR * (t + 1) / nthreads));
+        }
+        ft_zero(N, &w);
+        for (int t = 0; t < nthreads; ++t) {
+            for (size_t i = 0; i < NN; ++i) w.Hk[i] += tw[t].Hk[i];
+            for (size_t i = 0; i < 3 * NN; ++i) {
+                w.Hka[i] += tw[t].Hka[i];
+                w.Aka[i] += tw[t].Aka[i];
+            }
+            for (size_t i = 0; i < 9 * NN; ++i) w.Omk[i] += tw[t].Omk[i];
+        }
+        int rc = interp_after_ft(md, &w, Abar);
+        if (rc != 0) {
+            err = rc;
+            break;
+        }
+        band_sums(md, &jl, &w, out->Ne_sum, out->ahc, out->mep_ic, out->mep_lc, out->mep_cs, out->kubo_mep_ic,
+                  out->kubo_mep_lc, out->kubo_mep_cs, omega ? (zc *)out->velo_ahc : 0,
+                  omega ? (zc *)out->kubo_ohc : 0);
+        out->n_k += 1;
+    }
+    for (int t = 0; t < nthreads; ++t) ws_free(&tw[t]);
+    free(tw);
+    free(Abar);
+    ws_free(&w);
     return err;
 }
 

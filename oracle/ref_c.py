@@ -89,6 +89,8 @@ def lib():
         _LIB.oracle_run.restype = C.c_int
         _LIB.oracle_run.argtypes = [C.POINTER(_Model), C.POINTER(_Job), C.c_int64, C.c_int64,
                                     C.c_int64, C.POINTER(_Out), C.c_int]
+        _LIB.oracle_run_kserial.restype = C.c_int
+        _LIB.oracle_run_kserial.argtypes = _LIB.oracle_run.argtypes
         _LIB.oracle_interp_k.restype = C.c_int
     return _LIB
 
@@ -121,8 +123,13 @@ def _fortran_model(model: dict):
     return m, keep
 
 
-def run(model: dict, job: dict, k_begin: int = 0, k_count=None, k_stride: int = 1, nthreads: int = 0) -> dict:
-    """Same contract as ref_numpy.run, over k = k_begin + s*k_stride."""
+def run(model: dict, job: dict, k_begin: int = 0, k_count=None, k_stride: int = 1, nthreads: int = 0,
+        kserial: bool = False) -> dict:
+    """Same contract as ref_numpy.run, over k = k_begin + s*k_stride.
+
+    ``kserial=False``: threads share the k-points (OpenMP over k).
+    ``kserial=True``: the reference's own structure -- a serial k-loop with the
+    Fourier sum of each k split over the threads by R (oracle_run_kserial)."""
     L = lib()
     m, keep = _fortran_model(model)
     mp = [int(x) for x in job["mp_grid"]]
@@ -155,7 +162,8 @@ def run(model: dict, job: dict, k_begin: int = 0, k_count=None, k_stride: int = 
     for key in res:
         setattr(o, key, res[key].ctypes.data)
     o.n_k = 0
-    rc = L.oracle_run(C.byref(m), C.byref(j), int(k_begin), int(k_count), int(k_stride), C.byref(o), int(nthreads))
+    fn = L.oracle_run_kserial if kserial else L.oracle_run
+    rc = fn(C.byref(m), C.byref(j), int(k_begin), int(k_count), int(k_stride), C.byref(o), int(nthreads))
     if rc != 0:
         raise RuntimeError(f"oracle_run failed with status {rc}")
     res["n_k"] = int(o.n_k)

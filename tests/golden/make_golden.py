@@ -2,7 +2,7 @@
 
 Run in a checkout that has the reference next to it:
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py <path to the reference checkout>
 
 The reference ships, for the FeMn 3Q tight-binding model at strains
 delta = 0.9 / 1.0 / 1.1 (config/FeMn_TB/delta*/):
@@ -11,6 +11,9 @@ delta = 0.9 / 1.0 / 1.1 (config/FeMn_TB/delta*/):
 * ``FeMn_d*.latt``          the lattice (3 rows = a1, a2, a3, bohr)
 * ``ahc_tens.npy``          sigma_ab (3x3, atomic units) from kubo_ahc_tens
 * ``ahcVELO_sol*.npy``      velo_ahc_tens over 121 photon energies (3x3x121)
+
+The delta = 0.9 ``FeMn_hr.dat`` is also kept byte for byte (``hr_dat_0p900``,
+uint8), so the package's reader is tested on the reference's own file.
 
 The wf centres, N_val = 4, E_F = 0, T = 0, kuboTol = 1e-5 and eta = 0.1 eV are the
 ones tests/test_FeMn_AHE.f90:127-217 writes into input.cfg.  The file is parsed
@@ -58,10 +61,15 @@ def main(ref_root):
         out["latt_" + key] = np.loadtxt(os.path.join(base, latt_name))
         out["ahc_" + key] = np.load(os.path.join(base, "ahc_tens.npy"))
         out["ahcvelo_hw0_" + key] = np.load(os.path.join(base, velo_name))[:, :, 0]
+        if tag == "0.900":
+            with open(os.path.join(base, "w90files", "FeMn_hr.dat"), "rb") as fh:
+                out["hr_dat_" + key] = np.frombuffer(fh.read(), np.uint8)
     dst = os.path.join(os.path.dirname(os.path.abspath(__file__)), "femn.npz")
     np.savez_compressed(dst, **out)
     print("wrote", dst)
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <path to the reference checkout>")
+    main(sys.argv[1])

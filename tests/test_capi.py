@@ -134,6 +134,35 @@ def test_null_contexts_and_bad_counts_are_rejected(lib):
     assert lib.mepi_run_batch(2, None, None, None, None) == api.ERR_ARG
 
 
+def test_bandsum_noalloc_checks_arguments_before_device_work(lib):
+    """mepi_bandsum_noalloc answers bad arguments on the host, before any CUDA
+    call: a Fermi-energy count whose 32-bit slice size would wrap
+    (37 * 116080198 = 30 mod 2^32) and any count beyond the fixed scratch
+    array give MEPI_ERR_SCRATCH; an unsupported output bit, a non-finite
+    temperature and a negative kuboTol give MEPI_ERR_ARG.  The device pointers
+    are never dereferenced on these paths."""
+    f = lib.mepi_bandsum_noalloc
+    f.argtypes = [C.c_int32, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_double,
+                  C.c_int32, C.c_uint32, C.c_double, C.c_void_p, C.c_void_p]
+    f.restype = C.c_int
+    fake = C.c_void_p(0x1000)   # stands in for device buffers; never touched
+
+    def call(n_eF=1, T=0.0, nval=4, outputs=7, tol=1e-5):
+        return f(8, 1, fake, fake, None, n_eF, fake, T, nval, outputs, tol, fake, None)
+
+    err_scratch = 7
+    assert 37 * 116080198 % (1 << 32) == 30
+    assert call(n_eF=116080198) == err_scratch
+    assert call(n_eF=(1 << 31) - 1) == err_scratch
+    assert call(n_eF=91, nval=4) == err_scratch      # 37*91 + 27*4 = 3475 > 3449
+    assert call(outputs=8) == api.ERR_ARG            # optical Hall: not offered here
+    assert call(outputs=1 << 31) == api.ERR_ARG
+    assert call(T=float("inf")) == api.ERR_ARG
+    assert call(T=float("nan")) == api.ERR_ARG
+    assert call(tol=-1.0) == api.ERR_ARG
+    assert call(n_eF=0) == api.ERR_ARG
+
+
 def test_mlp_create_checks_shape_then_device(lib):
     """mepi_mlp_create rejects bad shapes (n_in 1..64, width 128, depth 1..8)
     with MEPI_ERR_ARG and, without a CUDA device, valid ones with

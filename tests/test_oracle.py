@@ -126,6 +126,20 @@ def test_numpy_vs_c(with_r, tb, gauge, sem, cart):
         assert rel(b[k], a[k]) < 1e-11, k
 
 
+def test_c_kserial_matches_kparallel():
+    """The reference-structured C variant (serial k-loop, Fourier sum split over
+    the threads by R) gives the k-parallel variant's sums, optical Hall
+    tensors included."""
+    m = random_tb_model(n_wf=8, r_max=1, seed=13).as_dict()
+    job = dict(mp_grid=(3, 3, 4), ef_lst=np.array([-0.02, 0.0]), T_kelvin=300.0, valence_bands=4,
+               hw_lst=np.array([0.0, 0.02]), eta_smr=0.004)
+    a = RC.run(m, job, nthreads=2)
+    b = RC.run(m, job, nthreads=3, kserial=True)
+    assert a["n_k"] == b["n_k"] == 36
+    for k in KEYS + ["velo_ahc", "kubo_ohc"]:
+        assert rel(b[k], a[k]) < 1e-12, k
+
+
 def test_optical_hall_numpy_vs_c():
     """velo_ahc_tens / kubo_ohc_tens (src/kubo.f90:86-198) in both restatements,
     and the hw = 0, eta -> velo form against the kubo_ahc curvature sum."""

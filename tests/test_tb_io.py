@@ -23,22 +23,40 @@ def test_hr_r_round_trip(tmp_path):
 
 
 def test_hr_reads_femn_layout(tmp_path):
+    """The reader on the reference's own FeMn_hr.dat (delta = 0.9), byte for
+    byte as shipped in config/FeMn_TB/delta0.900/w90files/: 8 Wannier
+    functions, 27 R vectors, H(R) equal to the fixture's independent parse."""
     g = np.load(GOLD)
-    H = g["H_eV_0p900"]
-    R = g["R_0p900"]
-    # write the fixture in the reference's layout (R, m fastest inside, m n Re Im)
     p = tmp_path / "FeMn_hr.dat"
-    with open(p, "w") as f:
-        f.write("FeMn\n8\n27\n")
-        f.write(" ".join(["1"] * 15) + "\n" + " ".join(["1"] * 12) + "\n")
-        for r in range(27):
-            for n in range(8):
-                for m in range(8):
-                    f.write(f"{R[r,0]} {R[r,1]} {R[r,2]} {m+1} {n+1} {H[r,m,n].real:.6f} {H[r,m,n].imag:.6f}\n")
+    p.write_bytes(g["hr_dat_0p900"].tobytes())
     Rb, Hb, deg = tb_io.read_hr_file(str(p))
-    assert deg.size == 27
-    assert np.allclose(Rb, R)
-    assert np.abs(Hb * AU_TO_EV - H).max() < 1e-6
+    assert deg.size == 27 and np.all(deg == 1)
+    assert np.array_equal(Rb, g["R_0p900"].astype(float))
+    assert np.abs(Hb * AU_TO_EV - g["H_eV_0p900"]).max() < 1e-12
+    # Hermitian model: H(-R) = H(R)^dag
+    idx = {tuple(r): i for i, r in enumerate(Rb.astype(int))}
+    for i, r in enumerate(Rb.astype(int)):
+        j = idx[tuple(-r)]
+        assert np.abs(Hb[j] - Hb[i].conj().T).max() < 1e-12
+
+
+def test_hr_warns_on_new_r_inside_block(tmp_path):
+    """An R vector that changes inside its block is a warning in the reference
+    (src/file_io.f90:720-727): the block keeps its first R and the element is
+    still stored."""
+    m = random_tb_model(n_wf=2, r_max=1, seed=2)
+    tb_io.write_hr_file(str(tmp_path / "x_hr.dat"), m)
+    lines = (tmp_path / "x_hr.dat").read_text().split("\n")
+    # second matrix line of the first R block: give it another R
+    first = next(i for i, ln in enumerate(lines) if len(ln.split()) == 7)
+    parts = lines[first + 1].split()
+    parts[0] = str(int(parts[0]) + 5)
+    lines[first + 1] = " ".join(parts)
+    (tmp_path / "x_hr.dat").write_text("\n".join(lines))
+    with pytest.warns(RuntimeWarning, match="unexpected new R_vect"):
+        R, H, _ = tb_io.read_hr_file(str(tmp_path / "x_hr.dat"))
+    assert np.array_equal(R, m.R_frac)
+    assert np.abs(H - m.H).max() <= 1e-7 / AU_TO_EV + 1e-12 * np.abs(m.H).max()
 
 
 def test_r_file_order_mismatch(tmp_path):
