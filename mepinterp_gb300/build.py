@@ -19,7 +19,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libmepi_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["capi.cu", "ft.cu", "ft_tc.cu", "ft_sep.cu", "eig.cu", "rot.cu", "gauge.cu", "bandsum.cu", "mlp.cu"]
+SOURCES = ["capi.cu", "ft.cu", "ft_tc.cu", "ft_sep.cu", "eig.cu", "rot.cu", "rot_tc.cu", "gauge.cu", "bandsum.cu", "mlp.cu"]
 
 
 def _nvcc() -> str:

@@ -69,7 +69,7 @@ struct mepi_ctx {
     double a_latt[9];
     DevBuf S, R, tau;
     // per-chunk work buffers
-    DevBuf W, E, E64, H64, U, HA, OD, V, CSV, ODH, flags, klist, kpts, partials, out, counters;
+    DevBuf W, E, E64, H64, U, Ulo, HA, OD, V, CSV, ODH, flags, klist, kpts, partials, out, counters;
     // explicit k lists (mepi_job.k_list) and the per-k output (mepi_acc.perk)
     DevBuf jlist, kpos, rpos, perk;
     std::vector<int64_t> kpos_host;     // job position of each kcol_host entry
@@ -82,6 +82,7 @@ struct mepi_ctx {
     std::vector<cplx<double>> S_host;  // FP64 stack, kept to build the tensor-core operands
     TcPlan tc;
     int ft_pref = 0;                    // MEPI_FT: 0 auto (separable when possible), 1 tensor core, 2 SIMT
+    int rot_pref = 0;                   // MEPI_ROT: 0 auto (tensor cores in the mixed form), 2 SIMT
     std::vector<double> R_host;         // lattice vectors, kept for the separable plan
     SepPlan sep;                        // separable-sum slabs of the current mesh
     bool sep_active = false;            // this run's chunks take the separable sums
@@ -176,7 +177,7 @@ template <typename T>
 size_t per_k_bytes(int N, int nb) {
     size_t NN = (size_t)N * N;
     return sizeof(cplx<T>) * (nb * NN + NN + 6 * NN + 3 * N + 3 * NN + 3 * N) + sizeof(T) * 2 * N + sizeof(int) +
-           sizeof(int64_t) + sizeof(double) * N + (sizeof(T) == 4 ? sizeof(cplx<double>) * NN : 0);
+           sizeof(int64_t) + sizeof(double) * N + (sizeof(T) == 4 ? (sizeof(cplx<double>) + sizeof(cplx<float>)) * NN : 0);
 }
 
 template <typename T>
@@ -187,6 +188,7 @@ int ensure_chunk(mepi_ctx* ctx, int64_t chunk) {
     CKM(ctx->E64.ensure(chunk * N * sizeof(double)));
     if (sizeof(T) == 4) CKM(ctx->H64.ensure(chunk * NN * sizeof(cplx<double>)));
     CKM(ctx->U.ensure(chunk * NN * sizeof(cplx<T>)));
+    if (sizeof(T) == 4) CKM(ctx->Ulo.ensure(chunk * NN * sizeof(cplx<float>)));   // refined vectors' low parts
     CKM(ctx->HA.ensure(chunk * 6 * NN * sizeof(cplx<T>)));
     CKM(ctx->OD.ensure(chunk * 3 * N * sizeof(cplx<T>)));
     CKM(ctx->V.ensure(chunk * 3 * NN * sizeof(cplx<T>)));
@@ -198,7 +200,7 @@ int ensure_chunk(mepi_ctx* ctx, int64_t chunk) {
 // device bytes of a context's separable slabs and per-chunk buffers
 size_t run_buffer_bytes(const mepi_ctx* ctx) {
     size_t b = ctx->sep.dev_bytes;
-    for (const DevBuf* d : {&ctx->W, &ctx->E, &ctx->E64, &ctx->H64, &ctx->U, &ctx->HA, &ctx->OD, &ctx->V, &ctx->CSV,
+    for (const DevBuf* d : {&ctx->W, &ctx->E, &ctx->E64, &ctx->H64, &ctx->U, &ctx->Ulo, &ctx->HA, &ctx->OD, &ctx->V, &ctx->CSV,
                             &ctx->flags})
         b += d->bytes;
     return b;
@@ -206,7 +208,7 @@ size_t run_buffer_bytes(const mepi_ctx* ctx) {
 
 void release_run_buffers(mepi_ctx* ctx) {
     cudaStreamSynchronize(ctx->stream);
-    for (DevBuf* d : {&ctx->W, &ctx->E, &ctx->E64, &ctx->H64, &ctx->U, &ctx->HA, &ctx->OD, &ctx->V, &ctx->CSV,
+    for (DevBuf* d : {&ctx->W, &ctx->E, &ctx->E64, &ctx->H64, &ctx->U, &ctx->Ulo, &ctx->HA, &ctx->OD, &ctx->V, &ctx->CSV,
                       &ctx->flags})
         d->release();
     sep_plan_free(ctx->sep);
@@ -251,14 +253,23 @@ int run_chunk(mepi_ctx* ctx, const KRange& kr, const JobDev* jb, int n_cta, doub
                                      ctx->U.as<cplx<T>>(), 40, counters, counters + 2, degen_gap, flags, ctx->stream,
                                      ctx->tune.jacobi_threads, ctx->tune.jacobi_kblock)));
         STAGE(ST_REFINE, launch_refine(ctx->N, nk, H64, reinterpret_cast<const float*>(ctx->E.p),
-                                       reinterpret_cast<cplx<float>*>(ctx->U.p), E64, degen_gap, flags, ctx->stream));
+                                       reinterpret_cast<cplx<float>*>(ctx->U.p), ctx->Ulo.as<cplx<float>>(), E64,
+                                       degen_gap, flags, ctx->stream));
     } else {
         STAGE(ST_EIG, (launch_eig<T>(ctx->N, nk, ctx->W.as<cplx<T>>(), ctx->nb, nullptr, reinterpret_cast<T*>(E64),
                                      ctx->U.as<cplx<T>>(), 40, counters, counters + 1, degen_gap, flags, ctx->stream,
                                      ctx->tune.jacobi_threads, ctx->tune.jacobi_kblock)));
     }
-    STAGE(ST_ROT, (launch_rot<T>(ctx->dm, nk, ctx->W.as<cplx<T>>(), ctx->U.as<cplx<T>>(), ctx->HA.as<cplx<T>>(),
-                                 ctx->OD.as<cplx<T>>(), ctx->stream)));
+    if (mixed && ctx->rot_pref == 0 && rot_tc_supported(ctx->dm)) {
+        // tensor-core rotation; a timed-out wait raises counters[3]
+        STAGE(ST_ROT, launch_rot_tc(ctx->dm, nk, reinterpret_cast<const cplx<float>*>(ctx->W.p),
+                                    reinterpret_cast<const cplx<float>*>(ctx->U.p), ctx->Ulo.as<cplx<float>>(),
+                                    reinterpret_cast<cplx<float>*>(ctx->HA.p), reinterpret_cast<cplx<float>*>(ctx->OD.p),
+                                    counters + 3, ctx->stream));
+    } else {
+        STAGE(ST_ROT, (launch_rot<T>(ctx->dm, nk, ctx->W.as<cplx<T>>(), ctx->U.as<cplx<T>>(), ctx->HA.as<cplx<T>>(),
+                                     ctx->OD.as<cplx<T>>(), ctx->stream)));
+    }
     STAGE(ST_GAUGE, (launch_gauge<T>(ctx->dm, nk, E64, ctx->HA.as<cplx<T>>(), ctx->OD.as<cplx<T>>(),
                                      ctx->V.as<cplx<T>>(), ctx->CSV.as<T>(), odh, ctx->stream)));
     if (bandsum) {
@@ -433,7 +444,7 @@ int run_prepare(mepi_ctx* ctx, const mepi_job* job, const mepi_acc* out) {
         size_t free_b = 0, total_b = 0;
         CK(cudaMemGetInfo(&free_b, &total_b));
         size_t held = 0;
-        for (const DevBuf* d : {&ctx->W, &ctx->E, &ctx->E64, &ctx->H64, &ctx->U, &ctx->HA, &ctx->OD, &ctx->V,
+        for (const DevBuf* d : {&ctx->W, &ctx->E, &ctx->E64, &ctx->H64, &ctx->U, &ctx->Ulo, &ctx->HA, &ctx->OD, &ctx->V,
                                 &ctx->CSV, &ctx->flags})
             held += d->bytes;
         cbudget = (size_t)(0.8 * (double)(free_b + held));   // halved inside default_chunk
@@ -716,7 +727,9 @@ int finish_collect(mepi_ctx* ctx, mepi_acc* out) {
     out->n_k_fp64 = r.fp64 ? r.count : r.n_redo;
     out->eig_max_sweeps = hc[0];
     // counters[1] counts FP64 Jacobi launches that hit the sweep cap (an error);
-    // FP32 cap hits (counters[2]) were flagged and rerun in FP64.
+    // FP32 cap hits (counters[2]) were flagged and rerun in FP64; counters[3]
+    // is raised by a tensor-core rotation whose bounded wait timed out.
+    if (hc[3] != 0) return MEPI_ERR_CUDA;
     if (hc[1] > 0) return MEPI_ERR_EIG;
     return MEPI_OK;
 }
@@ -873,6 +886,9 @@ int mepi_create(mepi_ctx** out, const mepi_model* m) {
     // model and mesh allow them
     const char* ft_env = std::getenv("MEPI_FT");
     ctx->ft_pref = (ft_env && std::strcmp(ft_env, "tc") == 0) ? 1 : (ft_env && std::strcmp(ft_env, "simt") == 0) ? 2 : 0;
+    // MEPI_ROT=simt forces the CUDA-core rotation in the mixed form (comparisons)
+    const char* rot_env = std::getenv("MEPI_ROT");
+    ctx->rot_pref = (rot_env && std::strcmp(rot_env, "simt") == 0) ? 2 : 0;
     std::vector<double> Rh(3 * (size_t)nR);
     std::memcpy(Rh.data(), m->R_frac, Rh.size() * sizeof(double));
     if (ctx->S.ensure(S.size() * sizeof(cplx<double>)) != cudaSuccess) return fail(MEPI_ERR_NOMEM);
@@ -980,6 +996,7 @@ int mepi_interp_k(mepi_ctx* ctx, int32_t precision, int64_t n_k, const double* k
         }
         int hc[4];
         CK(cudaMemcpy(hc, ctx->counters.p, sizeof(hc), cudaMemcpyDeviceToHost));
+        if (hc[3] != 0) return MEPI_ERR_CUDA;
         if (ctx->tc.err) {
             int terr = 0;
             CK(cudaMemcpy(&terr, ctx->tc.err, sizeof(int), cudaMemcpyDeviceToHost));
@@ -1226,7 +1243,7 @@ int mepi_destroy(mepi_ctx* ctx) {
     if (!ctx) return MEPI_OK;
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
-    for (DevBuf* b : {&ctx->S, &ctx->R, &ctx->tau, &ctx->W, &ctx->E, &ctx->E64, &ctx->H64, &ctx->U, &ctx->HA,
+    for (DevBuf* b : {&ctx->S, &ctx->R, &ctx->tau, &ctx->W, &ctx->E, &ctx->E64, &ctx->H64, &ctx->U, &ctx->Ulo, &ctx->HA,
                       &ctx->OD, &ctx->V, &ctx->CSV,
                       &ctx->ODH, &ctx->flags, &ctx->klist, &ctx->kpts, &ctx->partials, &ctx->out, &ctx->counters,
                       &ctx->jlist, &ctx->kpos, &ctx->rpos, &ctx->perk, &ctx->kcol})

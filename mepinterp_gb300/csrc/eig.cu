@@ -25,6 +25,12 @@ namespace mepi {
 
 namespace {
 
+__device__ __forceinline__ void two_sum_f(float a, float b, float& s, float& e) {
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
 // Stop when ||offdiag(M)||_F <= 4 sqrt(N) eps ||H||_F (the rounding floor of the
 // off-diagonal entries); rotations with |M_pq| below skip * ||H||_F are skipped
 // (their phase e^{i phi} would not be unitary to working precision).
@@ -340,8 +346,8 @@ cudaError_t launch_eig(int N, int64_t nk, const cplx<T>* W, int nbW, const cplx<
 // energies.
 __global__ void __launch_bounds__(256) refine_kernel(int N, const cplx<double>* __restrict__ H64,
                                                      const float* __restrict__ lam, cplx<float>* __restrict__ U,
-                                                     double* __restrict__ E64, double degen_gap,
-                                                     int* __restrict__ redo_flag) {
+                                                     cplx<float>* __restrict__ Ulo, double* __restrict__ E64,
+                                                     double degen_gap, int* __restrict__ redo_flag) {
     extern __shared__ unsigned char smem_raw[];
     const int Np = N + (N & 1), NPP = Np * Np, h = Np / 2;
     double* rho = reinterpret_cast<double*>(smem_raw);
@@ -488,10 +494,35 @@ __global__ void __launch_bounds__(256) refine_kernel(int N, const cplx<double>* 
         int rank = 0;
         for (int j = 0; j < N; ++j) rank += (En[j] < en || (En[j] == en && j < n)) ? 1 : 0;
         E64[(size_t)k * N + rank] = en;
-        const float sc = (float)(1.0 / sqrt(Sn[n]));
-        for (int row = 0; row < N; ++row) {
-            const cplx<float> u = Us[row * Np + n] + Ps[row * Np + n];
-            U[(size_t)k * NN + row * N + rank] = mk(u.re * sc, u.im * sc);
+        if (!Ulo) {
+            const float sc = (float)(1.0 / sqrt(Sn[n]));
+            for (int row = 0; row < N; ++row) {
+                const cplx<float> u = Us[row * Np + n] + Ps[row * Np + n];
+                U[(size_t)k * NN + row * N + rank] = mk(u.re * sc, u.im * sc);
+            }
+        } else {
+            // the refined vector (u + U C) / |u + U C| as FP32 hi + lo: the sum by
+            // TwoSum, its norm in FP64, the scaling by TwoProduct (FMA)
+            double q = 0.0;
+            for (int row = 0; row < N; ++row) {
+                const cplx<float> a = Us[row * Np + n], b = Ps[row * Np + n];
+                const double re = (double)a.re + (double)b.re, im = (double)a.im + (double)b.im;
+                q += re * re + im * im;
+            }
+            const double scd = 1.0 / sqrt(q);
+            const float sch = (float)scd, scl = (float)(scd - (double)sch);
+            for (int row = 0; row < N; ++row) {
+                const cplx<float> a = Us[row * Np + n], b = Ps[row * Np + n];
+                float hr, er, hm, em;
+                two_sum_f(a.re, b.re, hr, er);
+                two_sum_f(a.im, b.im, hm, em);
+                const float pr = hr * sch, pm = hm * sch;
+                const float lr = fmaf(hr, sch, -pr) + (er * sch + hr * scl);
+                const float lm = fmaf(hm, sch, -pm) + (em * sch + hm * scl);
+                const float ur = pr + lr, um = pm + lm;   // renormalised pair
+                U[(size_t)k * NN + row * N + rank] = mk(ur, um);
+                Ulo[(size_t)k * NN + row * N + rank] = mk((pr - ur) + lr, (pm - um) + lm);
+            }
         }
     }
     __syncthreads();
@@ -504,8 +535,8 @@ size_t refine_smem_bytes(int N) {
            5 * Np * Np * sizeof(cplx<float>);
 }
 
-cudaError_t launch_refine(int N, int64_t nk, const cplx<double>* H64, const float* lam, cplx<float>* U, double* E64,
-                          double degen_gap, int* redo_flag, cudaStream_t s) {
+cudaError_t launch_refine(int N, int64_t nk, const cplx<double>* H64, const float* lam, cplx<float>* U,
+                          cplx<float>* Ulo, double* E64, double degen_gap, int* redo_flag, cudaStream_t s) {
     if (nk <= 0) return cudaSuccess;
     const size_t smem = refine_smem_bytes(N);
     cudaError_t e = cudaFuncSetAttribute(refine_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -513,7 +544,7 @@ cudaError_t launch_refine(int N, int64_t nk, const cplx<double>* H64, const floa
         e = cudaFuncSetAttribute(refine_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
                                  cudaSharedmemCarveoutMaxShared);
     if (e != cudaSuccess) return e;
-    refine_kernel<<<(unsigned)nk, N <= 16 ? 128 : 256, smem, s>>>(N, H64, lam, U, E64, degen_gap, redo_flag);
+    refine_kernel<<<(unsigned)nk, N <= 16 ? 128 : 256, smem, s>>>(N, H64, lam, U, Ulo, E64, degen_gap, redo_flag);
     return cudaGetLastError();
 }
 

@@ -405,11 +405,15 @@ cudaError_t launch_eig(int N, int64_t nk, const cplx<T>* W, int nbW, const cplx<
                        int max_sweeps, int* sweeps_max, int* flag_cap, double degen_gap, int* redo_flag,
                        cudaStream_t s, int threads = 0, int kblock = 0);
 cudaError_t launch_ft_h64(const DevModel& m, const KRange& kr, cplx<double>* H64, cudaStream_t s);
-cudaError_t launch_refine(int N, int64_t nk, const cplx<double>* H64, const float* lam, cplx<float>* U, double* E64,
+cudaError_t launch_refine(int N, int64_t nk, const cplx<double>* H64, const float* lam, cplx<float>* U, cplx<float>* Ulo, double* E64,
                           double degen_gap, int* redo_flag, cudaStream_t s);
 template <typename T>
 cudaError_t launch_rot(const DevModel& m, int64_t nk, const cplx<T>* W, const cplx<T>* U, cplx<T>* HA,
                        cplx<T>* OD, cudaStream_t s);
+// tensor-core rotation of the mixed form (rot_tc.cu): n_wf <= 32 with the gauge transformation
+bool rot_tc_supported(const DevModel& m);
+cudaError_t launch_rot_tc(const DevModel& m, int64_t nk, const cplx<float>* W, const cplx<float>* U,
+                          const cplx<float>* Ulo, cplx<float>* HA, cplx<float>* OD, int* err, cudaStream_t s);
 template <typename T>
 cudaError_t launch_gauge(const DevModel& m, int64_t nk, const double* E, const cplx<T>* HA, const cplx<T>* OD,
                          cplx<T>* V, T* CSV, cplx<T>* ODH, cudaStream_t s);

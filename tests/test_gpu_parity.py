@@ -97,6 +97,36 @@ def test_eigenvalues_fp64_large_n(gpu_lib, n_wf, r_max):
     _check_per_k(m, kp, batch=8)
 
 
+@pytest.mark.parametrize("rot", ["tc", "simt"])
+def test_per_k_mixed_nwf32(gpu_lib, monkeypatch, rot):
+    """Per-k results of the mixed form at N = 32 (FP32 per-k work, refined FP64
+    energies) against the oracle, with the tensor-core rotation (default) and
+    the CUDA-core one (MEPI_ROT=simt): energies within 1e-9 of max |E|, the
+    gauge-invariant velocity quantities within 2e-5 of their largest entry."""
+    if rot == "simt":
+        monkeypatch.setenv("MEPI_ROT", "simt")
+    m = random_tb_model(n_wf=32, r_max=3, decay=1.5, seed=37)
+    kp = np.random.default_rng(3).uniform(-0.5, 0.5, size=(48, 3))
+    _check_per_k(m, kp, precision=api.PREC_MIXED, e_tol=1e-9, v_tol=2e-5, batch=8)
+
+
+def test_rotation_tc_matches_simt_sums(gpu_lib, monkeypatch):
+    """The tensor-core rotation (exact-slice FP16 digit products) and the
+    CUDA-core one (Dot2 velocity blocks, FP32 connection and curvature) both
+    give mixed-form sums within 1e-6 of the oracle on a 6^3 mesh of an N = 32
+    model."""
+    m = random_tb_model(n_wf=32, r_max=2, decay=1.5, seed=41)
+    job = dict(mp_grid=(6, 6, 6), ef_lst=np.array([-0.01, 0.0, 0.01]), T_kelvin=300.0, valence_bands=16,
+               hw_lst=np.array([0.0, 0.01]), eta_smr=0.002)
+    tc = api.run(m, job, precision=api.PREC_MIXED)
+    monkeypatch.setenv("MEPI_ROT", "simt")
+    simt = api.run(m, job, precision=api.PREC_MIXED)
+    ref = O.run(m.as_dict(), job, batch=36)
+    check_sums(tc, ref, MIXED_TOL)
+    check_sums(simt, ref, MIXED_TOL)
+    _check_complex(tc, ref, MIXED_TOL)
+
+
 @pytest.mark.parametrize("with_r,tb,gauge,sem,cart", [
     (True, True, True, "ref", False), (False, True, True, "ref", False), (True, False, True, "ref", False),
     (True, True, False, "ref", False), (True, True, True, "paper", False), (True, True, True, "ref", True),
