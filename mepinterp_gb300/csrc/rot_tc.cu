@@ -27,7 +27,9 @@
 // (A_y, A_z, Om_1, Om_2) and (Om_3); GEMM2 tiles the rotated blocks of the
 // first two.  The transpose T -> T^dag happens as the GEMM1 accumulator is read:
 // TMEM lane n of warp quarter q holds row n of T_q, and its digits are stored
-// into column n of the GEMM2 operand rows.  The curvature diagonal
+// into column n of the GEMM2 operand rows.  The Hermitian W-gauge blocks are
+// read from their upper triangle by columns (coalesced) and turned into rows by
+// a warp-shuffle transpose.  The curvature diagonal
 // d_n = sum_i conj(U_in) T_in is a cross-lane sum of the GEMM1 rows.
 //
 // One CTA (8 warps; warp w reads TMEM lanes 32 (w % 4).. and the real
@@ -150,6 +152,24 @@ __device__ __forceinline__ float transpose_reduce(float (&v)[32], int lane) {
         }
     }
     return v[0];
+}
+
+// 32 x 32 transpose across the warp: lane l holds column l (v[r] = M(r, l))
+// on entry and row l (v[c] = M(l, c)) on exit -- five butterfly stages that
+// swap one index bit with one lane bit, all register indices static
+__device__ __forceinline__ void transpose32(float (&v)[32], int lane) {
+#pragma unroll
+    for (int s = 16; s >= 1; s >>= 1) {
+        const bool b = (lane & s) != 0;
+#pragma unroll
+        for (int a = 0; a < 32; ++a) {
+            if (a & s) continue;
+            const float send = b ? v[a] : v[a + s];
+            const float recv = __shfl_xor_sync(0xffffffffu, send, s);
+            v[a] = b ? recv : v[a];
+            v[a + s] = b ? v[a + s] : recv;
+        }
+    }
 }
 
 // 8 columns of the four level accumulators -> hi + lo per column
@@ -303,19 +323,29 @@ __global__ void __launch_bounds__(RT_THREADS, 2)
             float mx = 0.f;
 #pragma unroll
             for (int m = 0; m < 32; ++m) xv[m] = 0.f;
-            if (present && n < N) {
-                // only the component this warp needs: Re (h = 0) or Im (h = 1); the
-                // Hermitian block from its upper triangle, X(n,m) = conj(X(m,n)) for m < n
+            if (present) {
+                // only the component this warp needs, Re (h = 0) or Im (h = 1).  The
+                // block's upper triangle U' (diagonal halved for Re, zero for Im) is
+                // read by columns, lane n holding U'(m, n) for every m (one coalesced
+                // load per m), and transposed across the warp to the rows U'(n, m);
+                // row n of the Hermitian block is then X_r = U'_r + U'_r^T,
+                // X_i = U'_i - U'_i^T.
                 const float* Wf = reinterpret_cast<const float*>(W + ((size_t)k * nbW + 1 + blk) * NN) + h;
+                float tv[32];
 #pragma unroll
-                for (int m = 0; m < 32; ++m)
-                    if (m < N) xv[m] = Wf[2 * ((m >= n) ? n * N + m : m * N + n)];
-                if (h == 1) {
-#pragma unroll
-                    for (int m = 0; m < 32; ++m) xv[m] = m > n ? xv[m] : (m < n ? -xv[m] : 0.f);
+                for (int m = 0; m < 32; ++m) {
+                    float v = 0.f;
+                    if (m <= n && n < N) v = Wf[2 * (m * N + n)];
+                    if (m == n) v = h == 0 ? 0.5f * v : 0.f;
+                    xv[m] = v;
+                    tv[m] = v;
                 }
+                transpose32(tv, lane);
 #pragma unroll
-                for (int m = 0; m < 32; ++m) mx = fmaxf(mx, fabsf(xv[m]));
+                for (int m = 0; m < 32; ++m) {
+                    xv[m] = h == 0 ? xv[m] + tv[m] : tv[m] - xv[m];
+                    mx = fmaxf(mx, fabsf(xv[m]));
+                }
             }
             S.half_max[h][row] = mx;
             __syncthreads();
@@ -404,9 +434,11 @@ __global__ void __launch_bounds__(RT_THREADS, 2)
             launch_mma();
             if (!(ok = wait_mma())) break;
             // ---- GEMM2 accumulator, lane m: Y_q(m, j) = 2^(e2_m + f_j - 16) (hi + lo) ----
-            float* stage = reinterpret_cast<float*>(Adig);   // [4 blocks][32 m][32 j][re, im]
+            // staged as real and imaginary planes [128 rows][33] (conflict-free row writes)
+            float* stage = reinterpret_cast<float*>(Adig);
             if (rot) {
                 const float pe2 = pow2f(S.a_exp[row]);
+                float* pl = stage + h * (128 * RT_LD) + row * RT_LD;
 #pragma unroll 1
                 for (int c = 0; c < 4; ++c) {
                     float hi[8], lo[8];
@@ -414,7 +446,7 @@ __global__ void __launch_bounds__(RT_THREADS, 2)
 #pragma unroll
                     for (int i = 0; i < 8; ++i) {
                         const int j = 8 * c + i;
-                        stage[(row * 32 + j) * 2 + h] = (hi[i] + lo[i]) * (pe2 * S.fsc[j]);
+                        pl[j] = (hi[i] + lo[i]) * (pe2 * S.fsc[j]);
                     }
                 }
             }
@@ -424,9 +456,9 @@ __global__ void __launch_bounds__(RT_THREADS, 2)
             // diagonal is real, so that the gauge commutators cancel as exactly as their terms
             for (int e = tid; e < nrot_tile * NN; e += RT_THREADS) {
                 const int bq = byNN.div(e), r = e - bq * NN, m = byN.div(r), j = r - m * N;
-                const float2* st = reinterpret_cast<const float2*>(stage) + bq * 1024;
-                const float2 v = m <= j ? st[m * 32 + j] : st[j * 32 + m];
-                HA[((size_t)k * 6 + 4 * tile + bq) * NN + r] = mk(v.x, m < j ? v.y : (m > j ? -v.y : 0.f));
+                const int o = (32 * bq + (m <= j ? m : j)) * RT_LD + (m <= j ? j : m);
+                const float vr = stage[o], vi = stage[128 * RT_LD + o];
+                HA[((size_t)k * 6 + 4 * tile + bq) * NN + r] = mk(vr, m < j ? vi : (m > j ? -vi : 0.f));
             }
         }
     }
