@@ -48,6 +48,13 @@ __device__ __forceinline__ void cross3(const cplx<T> a[3], const cplx<T> b[3], c
     out[2] = a[0] * b[1] - a[1] * b[0];
 }
 
+// acc -= a * b
+template <typename T>
+__device__ __forceinline__ void fms_c(cplx<T>& acc, cplx<T> a, cplx<T> b) {
+    acc.re = fma(-a.re, b.re, acc.re); acc.re = fma(a.im, b.im, acc.re);
+    acc.im = fma(-a.re, b.im, acc.im); acc.im = fma(-a.im, b.re, acc.im);
+}
+
 template <typename T>
 __device__ __forceinline__ T warp_sum(T v) {
 #pragma unroll
@@ -79,7 +86,204 @@ template <> struct CurvSum<float> {
     __device__ __forceinline__ double value() const { return (double)v.s + (double)v.c; }
 };
 
-template <typename T>
+// kGemm (FP32 form, N <= 32): the IC contraction of every (n, n0) pair,
+//     G_j(n, n0) = sum_{m != n0} (V(n,m) x W(m,n0))_j,  W(m,n0) = V(m,n0) / (E0 - Em),
+// is formed once per k-point as a register-tiled CUDA-core GEMM over m (2 x 2
+// (n, n0) tiles per thread, 24 FMA per (n, n0, m)) instead of inside the band
+// loop.  The Niu sum needs the same contraction without the terms whose product
+// denominator |(E0-En)^2 (E0-Em)| is within kuboTol: it equals G unless the
+// band nearest to n0 already fails that test (the rounded product is monotone
+// in |E0-Em|), and only for those (n0, n) pairs is it summed directly.
+constexpr int kMaskCap = 256;   // masked Niu pairs summed by whole warps per k-point
+
+// sum over the aligned group of 8 lanes
+__device__ __forceinline__ float sum8(float v) {
+    v += __shfl_xor_sync(0xffffffffu, v, 1);
+    v += __shfl_xor_sync(0xffffffffu, v, 2);
+    v += __shfl_xor_sync(0xffffffffu, v, 4);
+    return v;
+}
+__device__ __forceinline__ DF df_sum8(DF v) {
+#pragma unroll
+    for (int o = 1; o < 8; o <<= 1) {
+        const DF w{__shfl_xor_sync(0xffffffffu, v.s, o), __shfl_xor_sync(0xffffffffu, v.c, o)};
+        v = df_sum(v, w);
+    }
+    return v;
+}
+
+// Band-pair phase of the FP32 form for N <= 32, after the IC contraction G
+// (see bandsum_kernel): per band n0 the AHC curvature, the LC and IC terms,
+// Kubo (every n0) and Niu (n0 < valence_bands, kuboTol guard).
+//  1. the (n0, n) Niu pairs whose kuboTol window is not empty go to a compact
+//     list; a warp sums each one over m (lane = m) with the guard applied;
+//  2. eight threads per band n0 walk n = part, part + 8, ... and reduce their
+//     per-band tensors over the group of eight (three shuffle levels).
+__device__ __noinline__ void bandsum_pairs_gemm(const DevModel& md, const JobDev& jb, int N, int ld,
+                                                const cplx<float>* Vs, const cplx<float>* Ws, const cplx<float>* Gs,
+                                                cplx<float>* GVl, const float* dmin, int* s_list, short* s_map,
+                                                int& s_cnt, const float* Dt, const float* Iv, float* curvS,
+                                                float* curvC, float* icn, float* lcn, float* icv, float* lcv) {
+    const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nwarps = nt >> 5;
+    const int nval = jb.nval;
+    const float ttol = (float)md.kubo_tol;
+    auto V = [&](int a, int n, int m) -> cplx<float> { return Vs[(a * N + n) * ld + m]; };
+    auto W = [&](int a, int m, int n0) -> cplx<float> { return Ws[(a * 32 + m) * 33 + n0]; };
+    const bool mep = jb.do_mep && nval > 0;
+    if (tid == 0) s_cnt = 0;
+    __syncthreads();
+    if (mep) {
+        for (int t = tid; t < nval * N; t += nt) {
+            const int n0 = t / N, n = t - n0 * N;
+            short id = -1;
+            if (n != n0) {
+                const float d0n = Dt[n0 * N + n], a2 = d0n * d0n;
+                if (!(fabsf(a2 * dmin[n0]) > ttol)) {
+                    const int e = atomicAdd(&s_cnt, 1);
+                    if (e < kMaskCap) {
+                        s_list[e] = (n0 << 8) | n;
+                        id = (short)e;
+                    } else {
+                        id = -2;
+                    }
+                }
+            }
+            s_map[n0 * 32 + n] = id;
+        }
+    }
+    __syncthreads();
+    const int cnt = mep ? min(s_cnt, kMaskCap) : 0;
+    for (int e = warp; e < cnt; e += nwarps) {
+        const int n0 = s_list[e] >> 8, n = s_list[e] & 255;
+        const float d0n = Dt[n0 * N + n], a2 = d0n * d0n;
+        cplx<float> x[3] = {mk(0.f, 0.f), mk(0.f, 0.f), mk(0.f, 0.f)};
+        const int m = lane;
+        if (m < N && m != n0 && fabsf(a2 * Dt[n0 * N + m]) > ttol) {
+            cplx<float> vnm[3], wmo[3];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                vnm[c] = V(c, n, m);
+                wmo[c] = W(c, m, n0);
+            }
+            cross3(vnm, wmo, x);
+        }
+#pragma unroll
+        for (int c = 0; c < 3; ++c) x[c] = mk(warp_sum(x[c].re), warp_sum(x[c].im));
+        if (lane == 0) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) GVl[e * 3 + c] = x[c];
+        }
+    }
+    __syncthreads();
+    // eight threads per band n0
+    const int n0 = tid >> 3, part = tid & 7;
+    const bool live = n0 < N;
+    const bool niu = live && (n0 < nval) && jb.do_mep;
+    DF s_curv[9];
+    float s_ic[9], s_lc[9], s_icv[9], s_lcv[9];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+        s_curv[q] = DF{0.f, 0.f};
+        s_ic[q] = s_lc[q] = s_icv[q] = s_lcv[q] = 0.f;
+    }
+    if (live) {
+        cplx<float> vnn[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) vnn[c] = V(c, n0, n0);
+        for (int n = part; n < N; n += 8) {
+            if (n == n0) continue;
+            const float d0n = Dt[n0 * N + n];   // E0 - En
+            const float i0n = Iv[n0 * N + n];   // 1 / (E0 - En)
+            cplx<float> vi[3], vk[3];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) { vi[c] = V(c, n0, n); vk[c] = V(c, n, n0); }
+            if (jb.do_ahc) {
+                // the pair term formed once from (a, b) = (min, max): + to band a, - to band b
+                const int a = n0 < n ? n0 : n, b = n0 < n ? n : n0;
+                const float iab = Iv[a * N + b];
+                const float w = (n0 < n ? -2.f : 2.f) * iab * iab;
+                cplx<float> va[3], vb[3];
+#pragma unroll
+                for (int c = 0; c < 3; ++c) { va[c] = V(c, a, b); vb[c] = V(c, b, a); }
+#pragma unroll
+                for (int j = 0; j < 3; ++j)
+#pragma unroll
+                    for (int i = 0; i < 3; ++i) df_add(s_curv[i + 3 * j], w * (va[i] * vb[j]).im);
+            }
+            {   // LC
+                cplx<float> x[3];
+                cross3(vk, vnn, x);
+                const float den3 = d0n * d0n * d0n, i3 = i0n * i0n * i0n;
+                const bool kubo_ok = jb.do_kubo, niu_ok = niu && (fabsf(den3) > ttol);
+                if (kubo_ok || niu_ok) {
+#pragma unroll
+                    for (int j = 0; j < 3; ++j)
+#pragma unroll
+                        for (int i = 0; i < 3; ++i) {
+                            const float v = (vi[i] * x[j]).re * i3;
+                            if (kubo_ok) s_lc[i + 3 * j] += v;
+                            if (niu_ok) s_lcv[i + 3 * j] += v;
+                        }
+                }
+            }
+            if (jb.do_kubo || niu) {   // IC from the contraction G
+                cplx<float> g[3], gv[3];
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    g[c] = Gs[(c * 32 + n) * 33 + n0];
+                    gv[c] = mk(0.f, 0.f);
+                }
+                if (niu) {
+                    const int id = s_map[n0 * 32 + n];
+                    if (id == -1) {
+#pragma unroll
+                        for (int c = 0; c < 3; ++c) gv[c] = g[c];
+                    } else if (id >= 0) {
+#pragma unroll
+                        for (int c = 0; c < 3; ++c) gv[c] = GVl[id * 3 + c];
+                    } else {   // beyond the list's capacity: the guarded sum here
+                        const float a2 = d0n * d0n;
+                        for (int m = 0; m < N; ++m) {
+                            if (m == n0 || !(fabsf(a2 * Dt[n0 * N + m]) > ttol)) continue;
+                            cplx<float> vnm[3], wmo[3], x[3];
+#pragma unroll
+                            for (int c = 0; c < 3; ++c) {
+                                vnm[c] = V(c, n, m);
+                                wmo[c] = W(c, m, n0);
+                            }
+                            cross3(vnm, wmo, x);
+#pragma unroll
+                            for (int c = 0; c < 3; ++c) gv[c] = gv[c] + x[c];
+                        }
+                    }
+                }
+                const float ainv = i0n * i0n;
+#pragma unroll
+                for (int j = 0; j < 3; ++j)
+#pragma unroll
+                    for (int i = 0; i < 3; ++i) {
+                        s_ic[i + 3 * j] -= (vi[i] * g[j]).re * ainv;
+                        s_icv[i + 3 * j] -= (vi[i] * gv[j]).re * ainv;
+                    }
+            }
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+        const DF rf = df_sum8(s_curv[q]);
+        const float b = sum8(s_ic[q]), c = sum8(s_lc[q]), d = sum8(s_icv[q]), e = sum8(s_lcv[q]);
+        if (live && part == 0) {
+            curvS[q * N + n0] = rf.s;
+            curvC[q * N + n0] = rf.c;
+            icn[q * N + n0] = b;
+            lcn[q * N + n0] = c;
+            icv[q * kMaxN + n0] = d;
+            lcv[q * kMaxN + n0] = e;
+        }
+    }
+}
+
+template <typename T, bool kGemm>
 __global__ void __launch_bounds__(256) bandsum_kernel(DevModel md, JobDev jb, int64_t nk, const double* __restrict__ Eg,
                                                       const cplx<T>* __restrict__ Vg, const T* __restrict__ CSVg,
                                                       const int* __restrict__ skip, double* __restrict__ partials,
@@ -99,6 +303,14 @@ __global__ void __launch_bounds__(256) bandsum_kernel(DevModel md, JobDev jb, in
     T* Cs = lcv + 9 * kMaxN;                                      // [kMaxN]
     T* Dt = Cs + kMaxN;                                           // [N][N] E_a - E_b (difference formed in FP64)
     T* Iv = Dt + NN;                                              // [N][N] 1 / (E_a - E_b), 0 on the diagonal
+    // kGemm: W and G as [3][32][33] complex, and the nearest-band distance per band
+    cplx<T>* Ws = reinterpret_cast<cplx<T>*>((reinterpret_cast<uintptr_t>(Iv + NN) + 15) & ~uintptr_t(15));
+    cplx<T>* Gs = Ws + 3 * 32 * 33;
+    cplx<T>* GVl = Gs + 3 * 32 * 33;                              // [kMaskCap][3] masked Niu IC sums
+    T* dmin = reinterpret_cast<T*>(GVl + 3 * kMaskCap);
+    int* s_list = reinterpret_cast<int*>(dmin + 32);              // [kMaskCap] (n0 << 8) | n
+    short* s_map = reinterpret_cast<short*>(s_list + kMaskCap);   // [32][32] list index, -1 none, -2 over cap
+    __shared__ int s_cnt;
     const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nwarps = nt >> 5;
     const AccLayout L{nE, nval, jb.nW};
     double* P = partials + (size_t)blockIdx.x * L.size();
@@ -143,6 +355,62 @@ __global__ void __launch_bounds__(256) bandsum_kernel(DevModel md, JobDev jb, in
         }
         __syncthreads();
         auto V = [&](int a, int n, int m) -> cplx<T> { return Vs[(a * N + n) * ld + m]; };
+        if constexpr (kGemm) {
+            if (jb.do_kubo || (jb.do_mep && nval > 0)) {
+                for (int e = tid; e < 3 * 32 * 32; e += nt) {
+                    const int l = e >> 10, m = (e >> 5) & 31, n0 = e & 31;
+                    cplx<T> w = mk((T)0, (T)0);
+                    if (m < N && n0 < N && m != n0) w = Iv[n0 * N + m] * V(l, m, n0);
+                    Ws[(l * 32 + m) * 33 + n0] = w;
+                }
+                for (int n0 = tid; n0 < N; n0 += nt) {
+                    T dm = (T)1e30;
+                    for (int m = 0; m < N; ++m)
+                        if (m != n0) dm = fmin(dm, (T)fabs(Dt[n0 * N + m]));
+                    dmin[n0] = dm;
+                }
+                __syncthreads();
+                for (int t = tid; t < 256; t += nt) {
+                    const int nb = 2 * (t >> 4), ob = 2 * (t & 15);
+                    cplx<T> acc[2][2][3];
+#pragma unroll
+                    for (int i = 0; i < 2; ++i)
+#pragma unroll
+                        for (int jj = 0; jj < 2; ++jj)
+#pragma unroll
+                            for (int c = 0; c < 3; ++c) acc[i][jj][c] = mk((T)0, (T)0);
+                    for (int m = 0; m < N; ++m) {
+                        cplx<T> a[2][3], b[2][3];
+#pragma unroll
+                        for (int c = 0; c < 3; ++c) {
+#pragma unroll
+                            for (int i = 0; i < 2; ++i) a[i][c] = (nb + i < N) ? V(c, nb + i, m) : mk((T)0, (T)0);
+#pragma unroll
+                            for (int jj = 0; jj < 2; ++jj) b[jj][c] = Ws[(c * 32 + m) * 33 + ob + jj];
+                        }
+#pragma unroll
+                        for (int i = 0; i < 2; ++i)
+#pragma unroll
+                            for (int jj = 0; jj < 2; ++jj) {
+                                // (a x b)_j = a_k b_l - a_l b_k, (j,k,l) cyclic
+                                fma_c(acc[i][jj][0], a[i][1], b[jj][2]);
+                                fms_c(acc[i][jj][0], a[i][2], b[jj][1]);
+                                fma_c(acc[i][jj][1], a[i][2], b[jj][0]);
+                                fms_c(acc[i][jj][1], a[i][0], b[jj][2]);
+                                fma_c(acc[i][jj][2], a[i][0], b[jj][1]);
+                                fms_c(acc[i][jj][2], a[i][1], b[jj][0]);
+                            }
+                    }
+#pragma unroll
+                    for (int i = 0; i < 2; ++i)
+#pragma unroll
+                        for (int jj = 0; jj < 2; ++jj)
+#pragma unroll
+                            for (int c = 0; c < 3; ++c) Gs[(c * 32 + nb + i) * 33 + ob + jj] = acc[i][jj][c];
+                }
+                __syncthreads();
+            }
+        }
         // energy differences (formed in FP64) and their inverses: tabulated when
         // they fit in shared memory, else formed on the fly
         auto dE = [&](int a, int b) -> T { return use_tab ? Dt[a * N + b] : (T)(Es[a] - Es[b]); };
@@ -150,7 +418,11 @@ __global__ void __launch_bounds__(256) bandsum_kernel(DevModel md, JobDev jb, in
             return use_tab ? Iv[a * N + b] : (a == b ? (T)0 : (T)1 / (T)(Es[a] - Es[b]));
         };
 
-        for (int n0 = warp; n0 < N; n0 += nwarps) {
+        if constexpr (kGemm && sizeof(T) == 4) {
+            bandsum_pairs_gemm(md, jb, N, ld, Vs, Ws, Gs, GVl, dmin, s_list, s_map, s_cnt, Dt, Iv, curvS, curvC, icn,
+                               lcn, icv, lcv);
+        }
+        for (int n0 = warp; n0 < (kGemm ? 0 : N); n0 += nwarps) {
             const bool niu = (n0 < nval) && jb.do_mep;
             // per-band curvature: FP64 in the FP64 form, double-FP32 (TwoSum) in
             // the FP32 form, so that the pair terms of two occupied bands still
@@ -218,7 +490,30 @@ __global__ void __launch_bounds__(256) bandsum_kernel(DevModel md, JobDev jb, in
 #pragma unroll
                     for (int c = 0; c < 3; ++c) g[c] = gv[c] = mk((T)0, (T)0);
                     const T a2 = d0n * d0n;
-                    for (int m = 0; m < N; ++m) {
+                    if constexpr (kGemm) {
+#pragma unroll
+                        for (int c = 0; c < 3; ++c) g[c] = Gs[(c * 32 + n) * 33 + n0];
+                        if (niu) {
+                            if (fabs(a2 * dmin[n0]) > ttol) {
+#pragma unroll
+                                for (int c = 0; c < 3; ++c) gv[c] = g[c];
+                            } else {
+                                for (int m = 0; m < N; ++m) {
+                                    if (m == n0 || !(fabs(a2 * dE(n0, m)) > ttol)) continue;
+                                    cplx<T> vnm[3], wmo[3], x[3];
+#pragma unroll
+                                    for (int c = 0; c < 3; ++c) {
+                                        vnm[c] = V(c, n, m);
+                                        wmo[c] = Ws[(c * 32 + m) * 33 + n0];
+                                    }
+                                    cross3(vnm, wmo, x);
+#pragma unroll
+                                    for (int c = 0; c < 3; ++c) gv[c] = gv[c] + x[c];
+                                }
+                            }
+                        }
+                    }
+                    for (int m = 0; m < (kGemm ? 0 : N); ++m) {
                         if (m == n0) continue;
                         cplx<T> vnm[3], vmo[3], x[3];
 #pragma unroll
@@ -536,13 +831,23 @@ cudaError_t launch_bandsum(const DevModel& m, const JobDev& j, int64_t nk, const
     if (nk <= 0) return cudaSuccess;
     const bool tables = bandsum_smem<T>(m.N, true) <= 227 * 1024;
     size_t smem = bandsum_smem<T>(m.N, tables);
-    cudaError_t e = cudaFuncSetAttribute(bandsum_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(bandsum_kernel<T>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                 cudaSharedmemCarveoutMaxShared);
-    if (e != cudaSuccess) return e;
-    bandsum_kernel<T><<<n_cta, 256, smem, s>>>(m, j, nk, E, V, CSV, skip, partials, tables ? 1 : 0);
-    return cudaGetLastError();
+    // the GEMM form of the IC contraction: FP32 form, N <= 32, with its W and G arrays
+    const bool gemm = sizeof(T) == 4 && m.N <= 32 && tables;
+    if (gemm)
+        smem += 16 + (2 * 3 * 32 * 33 + 3 * kMaskCap) * sizeof(cplx<T>) + 32 * sizeof(T) + kMaskCap * sizeof(int) +
+                32 * 32 * sizeof(short);
+    auto go = [&](auto kern) {
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+        if (e != cudaSuccess) return e;
+        kern<<<n_cta, 256, smem, s>>>(m, j, nk, E, V, CSV, skip, partials, tables ? 1 : 0);
+        return cudaGetLastError();
+    };
+    if constexpr (sizeof(T) == 4) {
+        if (gemm) return go(bandsum_kernel<T, true>);
+    }
+    return go(bandsum_kernel<T, false>);
 }
 
 template <typename T>
