@@ -72,7 +72,7 @@ __global__ void __launch_bounds__(256) jacobi_kernel(int N, int64_t nk, int kblo
                                                      int nbW, const cplx<double>* __restrict__ H64,
                                                      T* __restrict__ E, cplx<T>* __restrict__ U, int max_sweeps,
                                                      int* sweeps_max, int* flag_cap, double degen_gap,
-                                                     int* redo_flag) {
+                                                     int* redo_flag, float gap_theta) {
     constexpr int HP = NP / 2, LD = NP + 1, PL = NP * LD;
     extern __shared__ unsigned char smem_raw[];
     T* Mr = reinterpret_cast<T*>(smem_raw);
@@ -177,10 +177,30 @@ __global__ void __launch_bounds__(256) jacobi_kernel(int N, int64_t nk, int kblo
             }
             return cta_sum(o, red);
         };
+        // With gap_theta > 0 (the FP32 form, whose eigenpairs the FP64 residual
+        // refinement finishes to second order), a pair is rotated only while
+        // |M_pq| > gap_theta |M_pp - M_qq|: the refinement's error is then of
+        // order gap_theta^3.  Rounds in which no pair rotates are skipped, and
+        // a sweep without rotations ends the run.
+        const T gth = (T)gap_theta;
+        auto strong = [&](int p, int q) {
+            const T xr = Mr[p * LD + q], xi = Mi[p * LD + q];
+            const T g = sqrt(xr * xr + xi * xi);
+            return g > gskip && !(gth > (T)0 && g <= gth * fabs(Mr[q * LD + q] - Mr[p * LD + p]));
+        };
         int sweep = 0;
         // a warm start may already be converged: test before the first sweep
         bool converged = (N == 1) || (warm && off_norm() <= tol2);
+        if (!converged && warm && gth > (T)0) {
+            int any = 0;
+            for (int e = tid; e < N * N; e += nt) {
+                const int i = e / N, j = e % N;
+                if (i < j && strong(i, j)) any = 1;
+            }
+            converged = !__syncthreads_or(any);
+        }
         for (sweep = 0; sweep < max_sweeps && !converged; ++sweep) {
+            int rotated = 0;
             for (int r = 0; r < NP - 1; ++r) {
                 // 1. rotation parameters of the pairs of this round
                 if (tid < HP) {
@@ -193,7 +213,7 @@ __global__ void __launch_bounds__(256) jacobi_kernel(int N, int64_t nk, int kblo
                         const T app = Mr[p * LD + p], aqq = Mr[q * LD + q];
                         const T xr = Mr[p * LD + q], xi = Mi[p * LD + q];
                         const T g = sqrt(xr * xr + xi * xi);
-                        if (g > gskip) {
+                        if (g > gskip && !(gth > (T)0 && g <= gth * fabs(aqq - app))) {
                             const T theta = (aqq - app) / (2 * g);
                             const T t = (theta >= 0 ? (T)1 : (T)-1) / (fabs(theta) + sqrt((T)1 + theta * theta));
                             c = (T)1 / sqrt((T)1 + t * t);
@@ -209,7 +229,9 @@ __global__ void __launch_bounds__(256) jacobi_kernel(int N, int64_t nk, int kblo
                     s_rot[tid] = RotPar<T>{c, sn, pr, pi};
                     s_d0[tid] = d0; s_d1[tid] = d1; s_fix[tid] = fix;
                 }
-                __syncthreads();
+                // a round without any rotation changes nothing
+                if (!__syncthreads_or(tid < HP ? s_fix[tid] : 0)) continue;
+                rotated = 1;
                 // 2. M <- G^dag M G, one 2 x 2 block per (pair A, pair B)
                 for (int t = tid; t < HP * HP; t += nt) {
                     const int A = t / HP, B = t % HP;
@@ -252,7 +274,7 @@ __global__ void __launch_bounds__(256) jacobi_kernel(int N, int64_t nk, int kblo
                 }
                 __syncthreads();
             }
-            converged = off_norm() <= tol2;
+            converged = (gth > (T)0 && !rotated) || off_norm() <= tol2;
         }
         if (tid == 0) {
             atomicMax(sweeps_max, sweep);
@@ -296,7 +318,7 @@ __global__ void __launch_bounds__(256) jacobi_kernel(int N, int64_t nk, int kblo
 template <typename T>
 cudaError_t launch_eig(int N, int64_t nk, const cplx<T>* W, int nbW, const cplx<double>* H64, T* E, cplx<T>* U,
                        int max_sweeps, int* sweeps_max, int* flag_cap, double degen_gap, int* redo_flag,
-                       cudaStream_t s, int threads_req, int kblock_req) {
+                       cudaStream_t s, int threads_req, int kblock_req, float gap_theta) {
     if (nk <= 0) return cudaSuccess;
     // a run of consecutive k-points per CTA, each warm-started from its
     // neighbour's eigenvectors (consecutive k-points are mesh neighbours).  Eight
@@ -313,7 +335,7 @@ cudaError_t launch_eig(int N, int64_t nk, const cplx<T>* W, int nbW, const cplx<
             e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
         if (e != cudaSuccess) return e;
         kern<<<grid, threads, smem, s>>>(N, nk, kblock, W, nbW, H64, E, U, max_sweeps, sweeps_max, flag_cap, degen_gap,
-                                         redo_flag);
+                                         redo_flag, gap_theta);
         return cudaGetLastError();
     };
     if (N <= 8) return go(jacobi_kernel<T, 8>, 8, 64);
@@ -549,8 +571,8 @@ cudaError_t launch_refine(int N, int64_t nk, const cplx<double>* H64, const floa
 }
 
 template cudaError_t launch_eig<double>(int, int64_t, const cplx<double>*, int, const cplx<double>*, double*,
-                                        cplx<double>*, int, int*, int*, double, int*, cudaStream_t, int, int);
+                                        cplx<double>*, int, int*, int*, double, int*, cudaStream_t, int, int, float);
 template cudaError_t launch_eig<float>(int, int64_t, const cplx<float>*, int, const cplx<double>*, float*,
-                                       cplx<float>*, int, int*, int*, double, int*, cudaStream_t, int, int);
+                                       cplx<float>*, int, int*, int*, double, int*, cudaStream_t, int, int, float);
 
 }  // namespace mepi
