@@ -83,6 +83,7 @@ struct mepi_ctx {
     TcPlan tc;
     int ft_pref = 0;                    // MEPI_FT: 0 auto (separable when possible), 1 tensor core, 2 SIMT
     int rot_pref = 0;                   // MEPI_ROT: 0 auto (tensor cores in the mixed form), 2 SIMT
+    int jacobi_warp = 1;                // FP32 Jacobi for N <= 32: register-resident warp form (MEPI_JACOBI=smem: CTA form)
     float jacobi_theta = 0.f;           // FP32 Jacobi: rotate a pair while |M_pq| > theta |M_pp - M_qq| (0: to the FP32 floor)
     std::vector<double> R_host;         // lattice vectors, kept for the separable plan
     SepPlan sep;                        // separable-sum slabs of the current mesh
@@ -178,7 +179,8 @@ template <typename T>
 size_t per_k_bytes(int N, int nb) {
     size_t NN = (size_t)N * N;
     return sizeof(cplx<T>) * (nb * NN + NN + 6 * NN + 3 * N + 3 * NN + 3 * N) + sizeof(T) * 2 * N + sizeof(int) +
-           sizeof(int64_t) + sizeof(double) * N + (sizeof(T) == 4 ? (sizeof(cplx<double>) + sizeof(cplx<float>)) * NN : 0);
+           sizeof(int64_t) + sizeof(double) * N +
+           (sizeof(T) == 4 ? (sizeof(cplx<double>) + sizeof(cplx<float>)) * NN : 0);
 }
 
 template <typename T>
@@ -252,7 +254,8 @@ int run_chunk(mepi_ctx* ctx, const KRange& kr, const JobDev* jb, int n_cta, doub
             STAGE(ST_FTH, launch_ft_h64(ctx->dm, kr, H64, ctx->stream));
         STAGE(ST_EIG, (launch_eig<T>(ctx->N, nk, ctx->W.as<cplx<T>>(), ctx->nb, H64, ctx->E.as<T>(),
                                      ctx->U.as<cplx<T>>(), 40, counters, counters + 2, degen_gap, flags, ctx->stream,
-                                     ctx->tune.jacobi_threads, ctx->tune.jacobi_kblock, ctx->jacobi_theta)));
+                                     ctx->jacobi_warp == 2 ? 1 : ctx->tune.jacobi_threads, ctx->tune.jacobi_kblock,
+                                     ctx->jacobi_theta, ctx->jacobi_warp != 0)));
         STAGE(ST_REFINE, launch_refine(ctx->N, nk, H64, reinterpret_cast<const float*>(ctx->E.p),
                                        reinterpret_cast<cplx<float>*>(ctx->U.p), ctx->Ulo.as<cplx<float>>(), E64,
                                        degen_gap, flags, ctx->stream));
@@ -892,6 +895,8 @@ int mepi_create(mepi_ctx** out, const mepi_model* m) {
     ctx->rot_pref = (rot_env && std::strcmp(rot_env, "simt") == 0) ? 2 : 0;
     // MEPI_JACOBI_THETA overrides the FP32 Jacobi's gap-relative stop (0 = run to the FP32 floor)
     if (const char* th = std::getenv("MEPI_JACOBI_THETA")) ctx->jacobi_theta = (float)std::atof(th);
+    if (const char* jf = std::getenv("MEPI_JACOBI"))
+        ctx->jacobi_warp = std::strcmp(jf, "smem") == 0 ? 0 : (std::strcmp(jf, "warp3") == 0 ? 2 : 1);
     std::vector<double> Rh(3 * (size_t)nR);
     std::memcpy(Rh.data(), m->R_frac, Rh.size() * sizeof(double));
     if (ctx->S.ensure(S.size() * sizeof(cplx<double>)) != cudaSuccess) return fail(MEPI_ERR_NOMEM);

@@ -313,12 +313,285 @@ __global__ void __launch_bounds__(256) jacobi_kernel(int N, int64_t nk, int kblo
     }
 }
 
+// ---------------------------------------------------------------------------
+// Register-resident FP32 Jacobi for N <= 32 (the mixed form): one warp per
+// warm-start run of k-points, lane r holding row r of the matrix M and row r
+// of the eigenvector accumulator V in registers, so that a sweep touches no
+// shared memory and needs no block barrier.
+//
+// Ordering: the round-robin ("circle") schedule with the pairs of every round
+// in the fixed slots (2a, 2a+1).  Player positions 0..31 map to slots by
+// slot(p) = 2p (p <= 15), 2(31-p)+1 (p >= 16); position 0 is fixed and the
+// others move one position per round, so the 31 rounds of a sweep meet every
+// pair once and return to the starting order.  Columns live at register index
+// = slot and move one step along the fixed slot cycle after every round
+// (static register moves); rows stay in their lanes, each lane computing the
+// slot its row holds this round and the lane of its pair partner.  A round
+// rotates the 16 slot pairs: columns by static register indices, rows by
+// exchanging the partner lane's row with shuffles.  The rotation of a pair is the one of jacobi_kernel
+// (Rutishauser choice of t, G = [[c, s e^{i phi}], [-s e^{-i phi}, c]]); pairs
+// with a padded index (>= N) or |M_pq| below the skip threshold are left.
+namespace {
+
+__host__ __device__ constexpr int jw_slot(int p) { return p <= 15 ? 2 * p : 2 * (31 - p) + 1; }
+__host__ __device__ constexpr int jw_pos(int s) { return (s & 1) ? 31 - (s >> 1) : (s >> 1); }
+
+// v[slot(p)] <- v[slot(p-1)] for p = 2..31, v[slot(1)] <- v[slot(31)]
+__device__ __forceinline__ void jw_cycle(float (&v)[32]) {
+    const float t = v[jw_slot(31)];
+#pragma unroll
+    for (int p = 31; p >= 2; --p) v[jw_slot(p)] = v[jw_slot(p - 1)];
+    v[jw_slot(1)] = t;
+}
+
+// v[idx] for a run-time idx, by a five-level select tree on the index bits
+__device__ __forceinline__ float jw_pick(const float (&v)[32], int idx) {
+    float a[16];
+#pragma unroll
+    for (int j = 0; j < 16; ++j) a[j] = (idx & 1) ? v[2 * j + 1] : v[2 * j];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) a[j] = (idx & 2) ? a[2 * j + 1] : a[2 * j];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) a[j] = (idx & 4) ? a[2 * j + 1] : a[2 * j];
+#pragma unroll
+    for (int j = 0; j < 2; ++j) a[j] = (idx & 8) ? a[2 * j + 1] : a[2 * j];
+    return (idx & 16) ? a[1] : a[0];
+}
+
+constexpr int JW_LD = 33;
+constexpr int JW_SMEM_FLOATS = 4 * 32 * JW_LD + 16 * 4 + 3 * 32;   // per warp: H, V planes, pair parameters, E/rank/player
+
+template <int NW, int MB>
+__global__ void __launch_bounds__(32 * NW, MB) jacobi_warp_kernel(int N, int64_t nk, int kblock,
+                                                              const cplx<double>* __restrict__ H64,
+                                                              float* __restrict__ E, cplx<float>* __restrict__ U,
+                                                              int max_sweeps, int* sweeps_max, int* flag_cap,
+                                                              double degen_gap, int* redo_flag) {
+    extern __shared__ float jw_sm[];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    float* Hr = jw_sm + (size_t)w * JW_SMEM_FLOATS;
+    float* Hi = Hr + 32 * JW_LD;
+    float* Sr = Hi + 32 * JW_LD;   // sorted eigenvectors [component][band]: output and next warm start
+    float* Si = Sr + 32 * JW_LD;
+    float4* prm = reinterpret_cast<float4*>(Si + 32 * JW_LD);   // [16] (c, s, e^{i phi})
+    float* sE = reinterpret_cast<float*>(prm + 16);
+    int* sR = reinterpret_cast<int*>(sE + 32);
+    int* sP = sR + 32;
+    const unsigned FULL = 0xffffffffu;
+    const int NN = N * N;
+    const int p0 = jw_pos(lane);   // position of this lane's row at the start of a sweep
+    const int64_t chain = (int64_t)blockIdx.x * NW + w;
+    float mr[32], mi[32], vr[32], vi[32];
+    for (int jb = 0; jb < kblock; ++jb) {
+        const int64_t k = chain * kblock + jb;
+        if (k >= nk) break;
+        const bool warm = jb > 0;
+        // FP32 copy of the FP64 H(k), Hermitised from its upper triangle
+        const cplx<double>* Hk = H64 + (size_t)k * NN;
+        float part = 0.f;
+        for (int a = 0; a < 32; ++a) {
+            const int b = lane;
+            if (b >= a) {
+                float re = 0.f, im = 0.f;
+                if (b < N && a < N) {
+                    const cplx<double> x = Hk[a * N + b];
+                    re = (float)x.re;
+                    im = b == a ? 0.f : (float)x.im;
+                }
+                Hr[a * JW_LD + b] = re;
+                Hi[a * JW_LD + b] = im;
+                Hr[b * JW_LD + a] = re;
+                Hi[b * JW_LD + a] = -im;
+                part += (b == a ? 1.f : 2.f) * (re * re + im * im);
+            }
+        }
+        __syncwarp();
+        float fro2 = part;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) fro2 += __shfl_xor_sync(FULL, fro2, o);
+        const int pid = lane;   // band (player) of this lane's row; after whole sweeps also of column slot 'lane'
+        if (!warm) {
+#pragma unroll
+            for (int t = 0; t < 32; ++t) {
+                mr[t] = Hr[lane * JW_LD + t];
+                mi[t] = Hi[lane * JW_LD + t];
+                vr[t] = t == lane ? 1.f : 0.f;
+                vi[t] = 0.f;
+            }
+        } else {
+            // M = S^dag H S with S the previous k-point's sorted eigenvectors:
+            // lane s forms row s of S^dag H, then row s of M
+            float wr[32], wi[32];
+#pragma unroll
+            for (int j = 0; j < 32; ++j) wr[j] = wi[j] = 0.f;
+            for (int i = 0; i < 32; ++i) {
+                const float a = Sr[i * JW_LD + lane], b = -Si[i * JW_LD + lane];   // conj(S_is)
+#pragma unroll
+                for (int j = 0; j < 32; ++j) {
+                    const float hr = Hr[i * JW_LD + j], hi = Hi[i * JW_LD + j];
+                    wr[j] = fmaf(a, hr, fmaf(-b, hi, wr[j]));
+                    wi[j] = fmaf(a, hi, fmaf(b, hr, wi[j]));
+                }
+            }
+#pragma unroll
+            for (int t = 0; t < 32; ++t) mr[t] = mi[t] = 0.f;
+#pragma unroll
+            for (int j = 0; j < 32; ++j) {
+                const float a = wr[j], b = wi[j];
+#pragma unroll
+                for (int t = 0; t < 32; ++t) {
+                    const float sr = Sr[j * JW_LD + t], si = Si[j * JW_LD + t];
+                    mr[t] = fmaf(a, sr, fmaf(-b, si, mr[t]));
+                    mi[t] = fmaf(a, si, fmaf(b, sr, mi[t]));
+                }
+            }
+#pragma unroll
+            for (int t = 0; t < 32; ++t) {
+                vr[t] = Sr[lane * JW_LD + t];
+                vi[t] = Si[lane * JW_LD + t];
+            }
+        }
+        // the diagonal of a Hermitian matrix is real
+#pragma unroll
+        for (int t = 0; t < 32; ++t) mi[t] = (t == lane) ? 0.f : mi[t];
+        const float tolr = 4.f * 1.1920928955078125e-07f * sqrtf((float)N);
+        const float tol2 = tolr * tolr * fro2;
+        const float gskip = 1e-10f * sqrtf(fro2);
+        // off-diagonal Frobenius norm, summed without the diagonal (subtracting d^2
+        // from the row sum would leave FP32 cancellation noise far above tol2)
+        auto off_norm = [&]() {
+            float o = 0.f;
+#pragma unroll
+            for (int t = 0; t < 32; ++t) o += (t == lane) ? 0.f : fmaf(mr[t], mr[t], mi[t] * mi[t]);
+#pragma unroll
+            for (int q = 16; q > 0; q >>= 1) o += __shfl_xor_sync(FULL, o, q);
+            return o;
+        };
+        bool converged = (N == 1) || (warm && off_norm() <= tol2);
+        int sweep = 0;
+        for (sweep = 0; sweep < max_sweeps && !converged; ++sweep) {
+            for (int r = 0; r < 31; ++r) {
+                // rows stay in their lanes: this lane's row sits at slot sl this round, its
+                // pair partner's row in lane pl (columns: register index = slot)
+                const int sl = jw_slot(p0 == 0 ? 0 : (p0 - 1 + r) % 31 + 1);
+                const int pqp = jw_pos(sl ^ 1);
+                const int pl = jw_slot(pqp == 0 ? 0 : (pqp - 1 - r + 62) % 31 + 1);
+                const bool even = !(sl & 1);
+                // pair (p, q) = (even slot, odd slot): parameters formed by the even lane
+                const float d = jw_pick(mr, sl);
+                const float xr0 = jw_pick(mr, sl ^ 1), xi0 = jw_pick(mi, sl ^ 1);
+                const float dq = __shfl_sync(FULL, d, pl);
+                float c = 1.f, sn = 0.f, pr = 1.f, pi = 0.f;
+                if (even && lane < N && pl < N) {
+                    const float app = d, aqq = dq, xr = xr0, xi = xi0;
+                    const float g = sqrtf(xr * xr + xi * xi);
+                    if (g > gskip) {
+                        const float th = (aqq - app) / (2.f * g);
+                        const float t = (th >= 0.f ? 1.f : -1.f) / (fabsf(th) + sqrtf(1.f + th * th));
+                        c = 1.f / sqrtf(1.f + t * t);
+                        sn = t * c;
+                        pr = xr / g;
+                        pi = xi / g;
+                    }
+                }
+                // (c, s e^{i phi}) of the pair
+                if (even) prm[sl >> 1] = make_float4(c, sn * pr, sn * pi, 0.f);
+                __syncwarp();
+                // M <- M G and V <- V G on this lane's rows (column pairs in static slots):
+                // p' = c x - s e^{-i phi} y,  q' = s e^{i phi} x + c y
+#pragma unroll
+                for (int a = 0; a < 16; ++a) {
+                    const float4 g4 = prm[a];
+                    const float ca = g4.x, zr = g4.y, zi = g4.z;
+                    {
+                        const float xr = mr[2 * a], xi = mi[2 * a], yr = mr[2 * a + 1], yi = mi[2 * a + 1];
+                        mr[2 * a] = fmaf(ca, xr, -fmaf(zr, yr, zi * yi));
+                        mi[2 * a] = fmaf(ca, xi, -fmaf(zr, yi, -zi * yr));
+                        mr[2 * a + 1] = fmaf(zr, xr, fmaf(-zi, xi, ca * yr));
+                        mi[2 * a + 1] = fmaf(zr, xi, fmaf(zi, xr, ca * yi));
+                    }
+                    {
+                        const float xr = vr[2 * a], xi = vi[2 * a], yr = vr[2 * a + 1], yi = vi[2 * a + 1];
+                        vr[2 * a] = fmaf(ca, xr, -fmaf(zr, yr, zi * yi));
+                        vi[2 * a] = fmaf(ca, xi, -fmaf(zr, yi, -zi * yr));
+                        vr[2 * a + 1] = fmaf(zr, xr, fmaf(-zi, xi, ca * yr));
+                        vi[2 * a + 1] = fmaf(zr, xi, fmaf(zi, xr, ca * yi));
+                    }
+                }
+                // M <- G^dag M on the pair's two rows:
+                // p' = c y_p - s e^{i phi} y_q,  q' = s e^{-i phi} y_p + c y_q
+                {
+                    const float4 g4 = prm[sl >> 1];
+                    const float ca = g4.x, A = even ? -g4.y : g4.y, B = g4.z;
+#pragma unroll
+                    for (int t = 0; t < 32; ++t) {
+                        const float orr = __shfl_sync(FULL, mr[t], pl), ori = __shfl_sync(FULL, mi[t], pl);
+                        mr[t] = fmaf(ca, mr[t], fmaf(A, orr, B * ori));
+                        mi[t] = fmaf(ca, mi[t], fmaf(A, ori, -B * orr));
+                    }
+                }
+                __syncwarp();
+                // next round: columns one step along the slot cycle (rows stay in their lanes)
+                jw_cycle(mr);
+                jw_cycle(mi);
+                jw_cycle(vr);
+                jw_cycle(vi);
+            }
+            converged = off_norm() <= tol2;
+        }
+        if (lane == 0) {
+            atomicMax(sweeps_max, sweep);
+            if (!converged) atomicAdd(flag_cap, 1);
+        }
+        // eigenvalues in slot order; ranks among the real bands (padded slots keep pid)
+        const float ev = jw_pick(mr, lane);
+        sE[lane] = ev;
+        sP[lane] = pid;
+        __syncwarp();
+        int rank = pid;
+        if (pid < N) {
+            rank = 0;
+            for (int t = 0; t < 32; ++t) {
+                if (sP[t] >= N) continue;
+                const float et = sE[t];
+                rank += (et < ev || (et == ev && t < lane)) ? 1 : 0;
+            }
+        }
+        sR[lane] = rank;
+        if (pid < N) E[(size_t)k * N + rank] = ev;
+        __syncwarp();
+        // sorted eigenvectors: S[i][rank(s)] = V[i][s]
+#pragma unroll
+        for (int t = 0; t < 32; ++t) {
+            const int rt = sR[t];
+            Sr[lane * JW_LD + rt] = vr[t];
+            Si[lane * JW_LD + rt] = vi[t];
+        }
+        __syncwarp();
+        for (int i = 0; i < N; ++i)
+            if (lane < N) U[(size_t)k * NN + i * N + lane] = mk(Sr[i * JW_LD + lane], Si[i * JW_LD + lane]);
+        if (redo_flag) {
+            // smallest gap between neighbouring sorted eigenvalues (H is free: sorted E in its first row)
+            if (pid < N) Hr[rank] = ev;
+            __syncwarp();
+            float gap = 1e30f;
+            if (lane + 1 < N) gap = Hr[lane + 1] - Hr[lane];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) gap = fminf(gap, __shfl_xor_sync(FULL, gap, o));
+            if (lane == 0) redo_flag[k] = (!converged || (double)gap < degen_gap || !(gap == gap)) ? 1 : 0;
+        }
+        __syncwarp();
+    }
+}
+
+}  // namespace
+
 }  // namespace
 
 template <typename T>
 cudaError_t launch_eig(int N, int64_t nk, const cplx<T>* W, int nbW, const cplx<double>* H64, T* E, cplx<T>* U,
                        int max_sweeps, int* sweeps_max, int* flag_cap, double degen_gap, int* redo_flag,
-                       cudaStream_t s, int threads_req, int kblock_req, float gap_theta) {
+                       cudaStream_t s, int threads_req, int kblock_req, float gap_theta, bool warp_form) {
     if (nk <= 0) return cudaSuccess;
     // a run of consecutive k-points per CTA, each warm-started from its
     // neighbour's eigenvectors (consecutive k-points are mesh neighbours).  Eight
@@ -338,6 +611,22 @@ cudaError_t launch_eig(int N, int64_t nk, const cplx<T>* W, int nbW, const cplx<
                                          redo_flag, gap_theta);
         return cudaGetLastError();
     };
+    if constexpr (sizeof(T) == 4) {
+        if (warp_form && H64 && N <= 32) {
+            constexpr int NW = 4;
+            const unsigned g = (unsigned)((nk + (int64_t)kblock * NW - 1) / ((int64_t)kblock * NW));
+            const size_t smem = (size_t)NW * JW_SMEM_FLOATS * sizeof(float);
+            auto wgo = [&](auto kern) {
+                cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+                if (e != cudaSuccess) return e;
+                kern<<<g, 32 * NW, smem, s>>>(N, nk, kblock, H64, reinterpret_cast<float*>(E),
+                                              reinterpret_cast<cplx<float>*>(U), max_sweeps, sweeps_max, flag_cap,
+                                              degen_gap, redo_flag);
+                return cudaGetLastError();
+            };
+            return threads_req == 1 ? wgo(jacobi_warp_kernel<NW, 3>) : wgo(jacobi_warp_kernel<NW, 1>);
+        }
+    }
     if (N <= 8) return go(jacobi_kernel<T, 8>, 8, 64);
     if (N <= 16) return go(jacobi_kernel<T, 16>, 16, 128);
     if (N <= 32) return go(jacobi_kernel<T, 32>, 32, 128);
@@ -571,8 +860,8 @@ cudaError_t launch_refine(int N, int64_t nk, const cplx<double>* H64, const floa
 }
 
 template cudaError_t launch_eig<double>(int, int64_t, const cplx<double>*, int, const cplx<double>*, double*,
-                                        cplx<double>*, int, int*, int*, double, int*, cudaStream_t, int, int, float);
+                                        cplx<double>*, int, int*, int*, double, int*, cudaStream_t, int, int, float, bool);
 template cudaError_t launch_eig<float>(int, int64_t, const cplx<float>*, int, const cplx<double>*, float*,
-                                       cplx<float>*, int, int*, int*, double, int*, cudaStream_t, int, int, float);
+                                       cplx<float>*, int, int*, int*, double, int*, cudaStream_t, int, int, float, bool);
 
 }  // namespace mepi

@@ -403,7 +403,8 @@ cudaError_t launch_ft_simt(const DevModel& m, const KRange& kr, cplx<T>* W, cuda
 template <typename T>
 cudaError_t launch_eig(int N, int64_t nk, const cplx<T>* W, int nbW, const cplx<double>* H64, T* E, cplx<T>* U,
                        int max_sweeps, int* sweeps_max, int* flag_cap, double degen_gap, int* redo_flag,
-                       cudaStream_t s, int threads = 0, int kblock = 0, float gap_theta = 0.f);
+                       cudaStream_t s, int threads = 0, int kblock = 0, float gap_theta = 0.f,
+                       bool warp_form = false);
 cudaError_t launch_ft_h64(const DevModel& m, const KRange& kr, cplx<double>* H64, cudaStream_t s);
 cudaError_t launch_refine(int N, int64_t nk, const cplx<double>* H64, const float* lam, cplx<float>* U, cplx<float>* Ulo, double* E64,
                           double degen_gap, int* redo_flag, cudaStream_t s);

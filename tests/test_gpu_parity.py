@@ -26,6 +26,16 @@ KEYS = ["Ne_sum", "ahc", "mep_ic", "mep_lc", "mep_cs", "kubo_mep_ic", "kubo_mep_
 GOLD = os.path.join(os.path.dirname(__file__), "golden", "femn.npz")
 E_TOL, SUM_TOL, MIXED_TOL = 1e-10, 1e-8, 1e-6
 TC_TOL = 2e-5   # FP32 accumulation over K = 2 nR inside the tensor core
+# The mixed form's Chern-Simons sums (mep_cs, kubo_mep_cs) on meshes or
+# subsets of a few hundred to a few thousand k-points.  Each k-point carries
+# FP32 noise of about 4e-7 of its own term (median; measured against the FP64
+# path, unbiased in sign), and these sums cancel 20- to 50-fold across k
+# (sum_k |t_k| / |sum_k t_k|), so on such samples the random walk of that noise
+# is 6e-7 to 9e-7 of the sum and single draws reach 1.6e-6.  On the full 128^3
+# mesh the walk averages out: test_mixed_full_mesh_partition holds every sum
+# of the whole mesh to MIXED_TOL against the FP64 path.
+MIXED_CS_TOL = 3e-6
+CS_KEYS = ("mep_cs", "kubo_mep_cs")
 
 
 def rel(a, b):
@@ -42,6 +52,13 @@ def check_sums(gpu, ref, tol, keys=KEYS):
     for k in keys:
         r = rel(gpu[k], ref[k])
         assert r < tol, f"{k}: rel err {r:.3e} (max |ref| {np.abs(ref[k]).max():.3e})"
+
+
+def check_mixed(gpu, ref, keys=KEYS):
+    """Mixed-form sums on a small mesh or a sampled subset: MIXED_TOL, the
+    Chern-Simons sums MIXED_CS_TOL."""
+    check_sums(gpu, ref, MIXED_TOL, keys=[k for k in keys if k not in CS_KEYS])
+    check_sums(gpu, ref, MIXED_CS_TOL, keys=[k for k in keys if k in CS_KEYS])
 
 
 def _check_complex(gpu, ref, tol, keys=("velo_ahc", "kubo_ohc")):
@@ -122,8 +139,8 @@ def test_rotation_tc_matches_simt_sums(gpu_lib, monkeypatch):
     monkeypatch.setenv("MEPI_ROT", "simt")
     simt = api.run(m, job, precision=api.PREC_MIXED)
     ref = O.run(m.as_dict(), job, batch=36)
-    check_sums(tc, ref, MIXED_TOL)
-    check_sums(simt, ref, MIXED_TOL)
+    check_mixed(tc, ref)
+    check_mixed(simt, ref)
     _check_complex(tc, ref, MIXED_TOL)
 
 
@@ -190,7 +207,7 @@ def test_odd_and_large_n(gpu_lib, n_wf):
     got = api.run(m, job, precision=api.PREC_FP64)
     check_sums(got, ref, SUM_TOL)
     mixed = api.run(m, job, precision=api.PREC_MIXED)
-    check_sums(mixed, ref, MIXED_TOL)
+    check_mixed(mixed, ref)
 
 
 def test_femn_golden_gpu(gpu_lib):
@@ -222,7 +239,7 @@ def test_mixed_config1(gpu_lib):
     ref = O.run(model.as_dict(), job, batch=512)
     got = api.run(model, job, precision=api.PREC_MIXED)
     assert got["n_k"] == 4096
-    check_sums(got, ref, MIXED_TOL)
+    check_mixed(got, ref)
     _check_complex(got, ref, MIXED_TOL)
 
 
@@ -232,24 +249,29 @@ def test_mixed_fermi_sweep(gpu_lib):
     job = dict(mp_grid=(6, 6, 6), ef_lst=ef, T_kelvin=290.1, valence_bands=6)
     ref = O.run(m.as_dict(), job)
     got = api.run(m, job, precision=api.PREC_MIXED)
-    check_sums(got, ref, MIXED_TOL)
+    check_mixed(got, ref)
 
 
 def test_mixed_full_mesh_partition(gpu_lib):
-    """nWf=32 model on its full 128^3 mesh in the mixed form: two round-robin
-    'ranks' sum to the single run (size-independent property), and a strided
-    subset agrees with the FP64 path."""
+    """nWf=32 model on its full 128^3 mesh in the mixed form: every sum of the
+    whole mesh within 1e-6 of the FP64 path on the same mesh (the accuracy
+    target of the mixed form), two round-robin 'ranks' sum to the single run
+    (size-independent property), and a strided subset agrees with the FP64
+    path."""
     model, job = workload("tb32_r3_k128")
     with api.Context(model) as ctx:
         full = ctx.core_worker_loc(job, precision=api.PREC_MIXED)
         assert full["n_k"] == 128 ** 3
+        full64 = ctx.core_worker_loc(job, precision=api.PREC_FP64)
+        check_sums(full, full64, MIXED_TOL)
+        _check_complex(full, full64, MIXED_TOL)
         parts = [ctx.core_worker_loc(job, precision=api.PREC_MIXED, k_begin=r, k_stride=2) for r in range(2)]
         for k in KEYS:
             assert rel(parts[0][k] + parts[1][k], full[k]) < 1e-9, k
         stride = 997
         a = ctx.core_worker_loc(job, precision=api.PREC_MIXED, k_stride=stride)
         b = ctx.core_worker_loc(job, precision=api.PREC_FP64, k_stride=stride)
-        check_sums(a, b, MIXED_TOL)
+        check_mixed(a, b)
 
 
 def test_mixed_config2_subset_vs_oracle(gpu_lib):
@@ -262,7 +284,7 @@ def test_mixed_config2_subset_vs_oracle(gpu_lib):
     ref = ref_c.run(model.as_dict(), job, k_begin=0, k_stride=stride)
     got = api.run(model, job, precision=api.PREC_MIXED, k_begin=0, k_stride=stride)
     assert got["n_k"] == ref["n_k"] == (128 ** 3 + stride - 1) // stride
-    check_sums(got, ref, MIXED_TOL)
+    check_mixed(got, ref)
     _check_complex(got, ref, MIXED_TOL)
 
 
@@ -315,7 +337,7 @@ def test_mixed_partial_ownership(gpu_lib):
     ref = O.run(m.as_dict(), job, k_indices=kidx)
     got = api.run(m, job, precision=api.PREC_MIXED, k_begin=2, k_stride=3, k_count=61)
     assert got["n_k"] == 61
-    check_sums(got, ref, MIXED_TOL)
+    check_mixed(got, ref)
     got64 = api.run(m, job, precision=api.PREC_FP64, k_begin=2, k_stride=3, k_count=61)
     check_sums(got64, ref, SUM_TOL)
 
@@ -337,13 +359,18 @@ def test_separable_slabs_under_memory_limit(gpu_lib, precision):
         assert t["ft_launches"] > t["eig_launches"], t
         ctx.set_mem_limit(0)
         again = ctx.core_worker_loc(job, precision=precision)
-    tol = SUM_TOL if precision == api.PREC_FP64 else MIXED_TOL
-    check_sums(lim, ref, tol)
-    _check_complex(lim, ref, tol)
-    # FP64: only the chunk boundaries move, so the sums agree to rounding; the
-    # mixed form's FP32 sums group the k-points of a CTA differently
-    check_sums(lim, free, 1e-12 if precision == api.PREC_FP64 else MIXED_TOL)
-    check_sums(again, free, 1e-12 if precision == api.PREC_FP64 else MIXED_TOL)
+    if precision == api.PREC_FP64:
+        check_sums(lim, ref, SUM_TOL)
+        _check_complex(lim, ref, SUM_TOL)
+        # only the chunk boundaries move, so the sums agree to rounding
+        check_sums(lim, free, 1e-12)
+        check_sums(again, free, 1e-12)
+    else:
+        # the mixed form's FP32 sums group the k-points of a CTA differently
+        check_mixed(lim, ref)
+        _check_complex(lim, ref, MIXED_TOL)
+        check_mixed(lim, free)
+        check_mixed(again, free)
 
 
 @pytest.mark.parametrize("T_kelvin,n_ef", [(0.0, 5), (290.1, 70)])
