@@ -69,13 +69,20 @@ def parse():
     p.add_argument("--chunk", type=int, default=0, help="k-points per chunk (0 = the library's default)")
     p.add_argument("--k-stride", type=int, default=1,
                    help="process every k-stride-th k-point of the mesh (small cases for profiling)")
-    p.add_argument("--form", choices=["kloop", "batched", "adaptive"], default="kloop",
+    p.add_argument("--form", choices=["kloop", "batched", "adaptive", "full"], default="kloop",
                    help="kloop: the headline k-loop (default); batched: many models in one CUDA graph launch; "
-                        "adaptive: learned-proposal refinement against uniform refinement")
+                        "adaptive: learned-proposal refinement against uniform refinement; full: the mixed form "
+                        "in a batched graph launch with the Fermi sweep, then learned refinement, on the largest "
+                        "workload (--workload tb64_r4_k256)")
     p.add_argument("--batch-models", type=int, default=64, help="batched form: number of models")
     p.add_argument("--no-autotune", action="store_true", help="batched form: skip the autotuner")
     p.add_argument("--coarse", type=int, default=48, help="adaptive form: coarse mesh edge")
     p.add_argument("--sub", type=int, default=6, help="adaptive form: sub-mesh edge per refined cell")
+    p.add_argument("--oracle-k", type=int, default=2048,
+                   help="full form: k-points (a stride of the mesh) on which the C oracle checks the mixed form")
+    p.add_argument("--refine-sub", type=int, default=2, help="full form: sub-mesh edge per refined cell")
+    p.add_argument("--refine-frac", type=float, default=0.005,
+                   help="full form: fraction of the cells the proposal selects (plus half as many sampled)")
     p.add_argument("--fp64-check", type=int, default=-1,
                    help="k-points on which the plain FP64 path is run for the error report and its own "
                         "throughput: -1 = the whole mesh (reusing the timed mixed result), N > 0 = a strided "
@@ -597,6 +604,136 @@ def run_adaptive(args, rank, world):
         print(json.dumps(out))
 
 
+def run_full(args, rank, world):
+    """The three forms together on one workload: the mixed form over the whole
+    mesh with its Fermi sweep in one batched CUDA-graph launch (mepi_run_batch,
+    launch shapes from the autotuner) with the per-k output, then learned
+    refinement of the cells the proposal network picks from that output.
+    Accuracy: the mixed form against the C oracle on a strided sample and
+    against the plain FP64 GPU path on a 64^3-point stride of the mesh; the
+    refinement's own effect is reported as the change it makes to the sums."""
+    import numpy as np
+    import torch
+    from mepinterp_gb300 import adaptive as AD
+    from mepinterp_gb300 import api
+    from mepinterp_gb300.generator import workload
+
+    model, job = workload(args.workload)
+    if args.mesh > 0:
+        job["mp_grid"] = (args.mesh,) * 3
+    mp = job["mp_grid"]
+    if len(set(mp)) != 1:
+        raise SystemExit("the full form refines cells of a cubic mesh")
+    n = int(mp[0])
+    n_tot = n ** 3
+    # the proposal follows each k-point's AHC term at the first Fermi energy of
+    # the job: put the sweep's energy closest to 0 first, and undo the order after
+    ef = np.asarray(job["ef_lst"], np.float64)
+    i0 = int(np.argmin(np.abs(ef)))
+    order = np.roll(np.arange(ef.size), -i0)
+    jobr = dict(job, ef_lst=ef[order])
+    inv = np.argsort(order)
+
+    def unroll(r):
+        out = dict(r)
+        for k in ("Ne_sum",):
+            out[k] = np.asarray(r[k])[inv]
+        for k in ("ahc", "kubo_mep_ic", "kubo_mep_lc", "kubo_mep_cs", "velo_ahc", "kubo_ohc"):
+            if k in r:
+                out[k] = np.asarray(r[k])[..., inv]
+        return out
+
+    mixed, fp64 = api.PREC_MIXED, api.PREC_FP64
+    ctx = api.Context(model)
+    t0 = time.perf_counter()
+    tuning = ctx.autotune(jobr, precision=mixed, sample_k=min(16384, n_tot))
+    tune_s = time.perf_counter() - t0
+    for _ in range(max(args.warmup, 3)):                    # a slice of the mesh: kernels, slabs, buffers
+        ctx.core_worker_loc(jobr, precision=mixed, k_count=min(65536, n_tot))
+    clocks = ClockSampler()
+    torch.cuda.synchronize()
+    clocks.start()
+    steps = []
+    for st in range(max(1, args.steps)):
+        t0 = time.perf_counter()
+        (main,), graph_ms = api.run_batch([ctx], [jobr], mixed, perk=True)
+        t1 = time.perf_counter()
+        ref = AD.adaptive(ctx, jobr, n=n, s=args.refine_sub, frac=args.refine_frac,
+                          sample_frac=0.5 * args.refine_frac, precision=mixed, seed=st, coarse=main)
+        t2 = time.perf_counter()
+        steps.append({"main_s": t1 - t0, "graph_ms": graph_ms, "refine_s": t2 - t1, "wall_s": t2 - t0})
+    clk = clocks.stop()
+    main_u, ref_u = unroll(main), unroll(ref)
+    n_eval = int(ref["n_k_evaluated"])
+    wall = statistics.median(s["wall_s"] for s in steps)
+
+    sxy = lambda r: float(np.asarray(r["ahc"])[0, 1, i0])
+    mep = lambda r: (np.asarray(r["mep_ic"]) + np.asarray(r["mep_lc"]) + np.asarray(r["mep_cs"])).sum(-1)
+    keys = ("ahc", "mep_ic", "mep_lc", "mep_cs", "kubo_mep_ic", "kubo_mep_lc", "kubo_mep_cs")
+
+    def errs(a, b):
+        e = {k: _rel_max(a[k], b[k]) for k in keys}
+        for k in ("velo_ahc", "kubo_ohc"):
+            if k in a and k in b:
+                e[k] = _rel_max(a[k], b[k])
+        e["sigma_xy_at_ef0"] = abs(sxy(a) - sxy(b)) / abs(sxy(b))
+        e["mep_tensor"] = _rel_max(mep(a), mep(b))
+        e["worst"] = max(v for v in e.values())
+        return e
+
+    # the mixed form against the plain FP64 GPU path on a 64^3-point stride of the mesh
+    st64 = max(1, n_tot // 64 ** 3)
+    t0 = time.perf_counter()
+    a64 = ctx.core_worker_loc(jobr, precision=mixed, k_stride=st64)
+    mixed_sub_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    b64 = ctx.core_worker_loc(jobr, precision=fp64, k_stride=st64)
+    fp64_sub_s = time.perf_counter() - t0
+    # ... and against the C oracle on a sparser stride
+    cpu = None
+    err_or = None
+    if rank == 0 and args.oracle_k > 0:
+        from oracle import ref_c
+        ref_c.build()
+        sto = max(1, n_tot // args.oracle_k)
+        ao = ctx.core_worker_loc(jobr, precision=mixed, k_stride=sto)
+        t0 = time.perf_counter()
+        bo = ref_c.run(model.as_dict(), jobr, k_begin=0, k_stride=sto)
+        cpu_s = time.perf_counter() - t0
+        err_or = dict(errs(ao, bo), k_points=int(ao["n_k"]), k_stride=sto)
+        cpu = {"value": bo["n_k"] / cpu_s, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+               "sample": f"{bo['n_k']} k-points (every {sto}th of the {n}^3 mesh), {cpu_s:.1f} s"}
+    ctx.close()
+    if rank == 0:
+        out = {
+            "metric": "k-points/s, full form (mixed + batched graph launch + learned refinement)",
+            "value": n_eval / wall, "unit": UNIT, "n_gpus": world, "steps": len(steps),
+            "warmup": max(args.warmup, 3), "ms_per_step": 1e3 * wall, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 (f64 H(k), eigen-residual, energies, k-sums) + bf16 proposal network",
+            "data": "synthetic (seeded random tight-binding model)",
+            "config": {"workload": args.workload, "n_wf": model.n_wf, "n_R": model.n_R, "mesh": list(mp),
+                       "n_eF": int(ef.size), "T_kelvin": job["T_kelvin"], "valence_bands": job["valence_bands"],
+                       "refine_sub": args.refine_sub, "refine_frac": args.refine_frac,
+                       "proposal_follows_ef_ev": float(ef[i0] * 27.211386245988),
+                       "warmup": "3 runs of the first 65,536 k-points", "parallelism": f"replicas x{world}"},
+            "k_points_evaluated": n_eval, "cells_refined": int(ref["cells_refined"]),
+            "steps_detail": steps,
+            "main_pass": {"value": n_tot / statistics.median(s["main_s"] for s in steps),
+                          "graph_value": n_tot / (1e-3 * statistics.median(s["graph_ms"] for s in steps)),
+                          "fp64_reruns": int(main["n_k_fp64"])},
+            "autotune": {"seconds": tune_s, "choice": tuning},
+            "refinement_change": errs(ref_u, main_u),
+            "error_vs_fp64": dict(errs(a64, b64), k_points=int(a64["n_k"]), k_stride=st64),
+            "fp64_path": {"value": b64["n_k"] / fp64_sub_s, "unit": UNIT, "k_points": int(b64["n_k"]),
+                          "mixed_value_same_points": a64["n_k"] / mixed_sub_s},
+            "error_vs_oracle": err_or,
+            "cpu_baseline": cpu,
+            "clocks": clk,
+        }
+        print(json.dumps(out))
+
+
 def main():
     args = parse()
     rank, world = dist_setup()
@@ -606,6 +743,8 @@ def main():
         run_batched(args, rank, world)
     elif args.form == "adaptive":
         run_adaptive(args, rank, world)
+    elif args.form == "full":
+        run_full(args, rank, world)
     else:
         run_gpu(args, rank, world)
     if world > 1:

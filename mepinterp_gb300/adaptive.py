@@ -108,18 +108,24 @@ def assemble(coarse: dict, parts) -> dict:
 
 def adaptive(ctx: api.Context, job: dict, n: int = 48, s: int = 6, frac: float = 0.02,
              sample_frac: float = 0.01, precision: int = api.PREC_MIXED, seed: int = 0, depth: int = 4,
-             epochs: int = 200, batch: int = 256, lr: float = 1e-3, selector: str = "mlp") -> dict:
+             epochs: int = 200, batch: int = 256, lr: float = 1e-3, selector: str = "mlp",
+             coarse: dict | None = None) -> dict:
     """Adaptive refinement of a job on the n^3 coarse mesh with s^3 sub-meshes.
 
     ``selector``: "mlp" (the learned proposal, default), "omega" (the coarse
     |Omega| alone), "random" (the same number of cells at random), or "none"
-    (the coarse mesh alone).  Returns the sums in the coarse mesh's
+    (the coarse mesh alone).  ``coarse``: the coarse pass's result with its
+    per-k output, when the caller has already run it (e.g. inside a batched
+    launch); else it is run here.  Returns the sums in the coarse mesh's
     normalisation (so ``output.integrate_over_k_space(res, (n, n, n), ...)``
     normalises them), with bookkeeping: k-points evaluated, cells refined,
     and the network's loss history.
     """
     rng = np.random.default_rng(seed)
-    coarse = ctx.core_worker_loc(_job(job, n), precision=precision, perk=True)
+    if coarse is None:
+        coarse = ctx.core_worker_loc(_job(job, n), precision=precision, perk=True)
+    elif "perk" not in coarse or len(coarse["perk"]) != n ** 3:
+        raise ValueError("the coarse result needs the per-k output of the whole n^3 mesh")
     perk = coarse["perk"]
     n_cells = n ** 3
     n_sel = int(round(frac * n_cells))

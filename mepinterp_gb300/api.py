@@ -327,12 +327,13 @@ class _JobCall:
         return res
 
 
-def run_batch(contexts, jobs, precision=PREC_MIXED):
+def run_batch(contexts, jobs, precision=PREC_MIXED, perk: bool = False):
     """mepi_run_batch: one (context, job) pair per model, all in one CUDA graph
-    launch.  ``precision`` is one value or one per job.  Returns (list of the
-    unnormalised local sums, device time of the graph in ms)."""
+    launch.  ``precision`` is one value or one per job; with ``perk`` every
+    result also holds "perk" (see :meth:`Context.core_worker_loc`).  Returns
+    (list of the unnormalised local sums, device time of the graph in ms)."""
     precs = precision if isinstance(precision, (list, tuple)) else [precision] * len(jobs)
-    calls = [_JobCall(j, p) for j, p in zip(jobs, precs)]
+    calls = [_JobCall(j, p, perk=perk) for j, p in zip(jobs, precs)]
     n = len(calls)
     lib = contexts[0].lib
     ctxs = (C.c_void_p * n)(*[c._h.value for c in contexts])

@@ -113,6 +113,7 @@ struct mepi_ctx {
         std::vector<int64_t> redo, redo_pos, rslab;
         int64_t rchunk = 0;
         bool sep_keep = false;
+        bool in_reruns = false;         // the FP64 reruns are being enqueued (scattered k-points)
     } run;
     double* h_out = nullptr;            // pinned copy-back of the reduced sums and counters
     size_t h_out_cap = 0;
@@ -260,9 +261,12 @@ int run_chunk(mepi_ctx* ctx, const KRange& kr, const JobDev* jb, int n_cta, doub
                                        reinterpret_cast<cplx<float>*>(ctx->U.p), ctx->Ulo.as<cplx<float>>(), E64,
                                        degen_gap, flags, ctx->stream));
     } else {
+        // the reruns' k-points are scattered over the mesh: a warm start from the
+        // previous one would not be a neighbour's, so one k-point per CTA (cold
+        // starts, and every CTA of the few hundred to few thousand runs at once)
         STAGE(ST_EIG, (launch_eig<T>(ctx->N, nk, ctx->W.as<cplx<T>>(), ctx->nb, nullptr, reinterpret_cast<T*>(E64),
                                      ctx->U.as<cplx<T>>(), 40, counters, counters + 1, degen_gap, flags, ctx->stream,
-                                     ctx->tune.jacobi_threads, ctx->tune.jacobi_kblock)));
+                                     ctx->tune.jacobi_threads, ctx->run.in_reruns ? 1 : ctx->tune.jacobi_kblock)));
     }
     if (mixed && ctx->rot_pref == 0 && rot_tc_supported(ctx->dm)) {
         // tensor-core rotation; a timed-out wait raises counters[3]
@@ -666,6 +670,7 @@ int finish_launch(mepi_ctx* ctx) {
     if (!r.redo.empty()) {
         if (!ctx->sep.ready || (!ctx->sep.whole() && r.rslab.empty())) ctx->sep_active = false;
         if (r.rslab.empty()) r.rslab = {0, (int64_t)r.redo.size()};
+        r.in_reruns = true;
         for (size_t j = 0; j + 1 < r.rslab.size(); ++j) {
             const int64_t b = r.rslab[j], e = r.rslab[j + 1];
             if (e <= b) continue;
@@ -676,9 +681,13 @@ int finish_launch(mepi_ctx* ctx) {
                           {job.mp_grid[0], job.mp_grid[1], job.mp_grid[2]}};
                 rc = run_chunk<double>(ctx, kr, &r.jb, r.n_cta, 0.0, false, true, nullptr);
                 if (!rc && r.perk) rc = enqueue_perk<double>(ctx, kr.count, ctx->rpos.as<int64_t>() + c0, 0);
-                if (rc) return rc;
+                if (rc) {
+                    r.in_reruns = false;
+                    return rc;
+                }
             }
         }
+        r.in_reruns = false;
         ctx->sep_active = r.sep_keep;
     }
     STAGE(ST_RED, launch_reduce(ctx->partials.as<double>(), r.n_cta, L.size(), ctx->out.as<double>(), ctx->stream));
