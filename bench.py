@@ -505,9 +505,12 @@ def run_batched(args, rank, world):
     seq = []
     for c in ctxs:
         c.trim()                      # the batch's buffers; each sequential run allocates its own
-    for c, j in zip(ctxs, jobs):
+    per_model = []
+    for (m, _), c, j in zip(work, ctxs, jobs):
         seq.append(c.core_worker_loc(j, precision=prec))
-        seq_dev_ms += c.timing()["run_ms"]
+        ms = c.timing()["run_ms"]
+        seq_dev_ms += ms
+        per_model.append([m.n_wf, m.n_R, int(j["mp_grid"][0]), round(ms, 1)])
         c.trim()
     seq_s = time.perf_counter() - t0
     diffs = [(_rel_max(a[k], b[k]), i, k) for i, (a, b) in enumerate(zip(res, seq))
@@ -527,7 +530,8 @@ def run_batched(args, rank, world):
                    "autotune": not args.no_autotune, "distinct_tuning_buckets": len(tuned)},
         "graph_ms_per_step": statistics.median(graph),
         "graph_value": nk / (statistics.median(graph) * 1e-3),
-        "sequential": {"value": nk / seq_s, "device_value": nk / (seq_dev_ms * 1e-3), "seconds": seq_s},
+        "sequential": {"value": nk / seq_s, "device_value": nk / (seq_dev_ms * 1e-3), "seconds": seq_s,
+                       "per_model_nwf_nr_edge_ms": per_model},
         "speedup_vs_sequential": (nk / (sum(wall) / args.steps)) / (nk / seq_s),
         "batch_vs_sequential_max_rel_diff": {"value": diff, "model": worst_model, "key": worst_key},
         "create_s": create_s, "autotune_s": tune_s, "clocks": clk,
