@@ -190,7 +190,7 @@ int ensure_chunk(mepi_ctx* ctx, int64_t chunk) {
     CKM(ctx->W.ensure(chunk * ctx->nb * NN * sizeof(cplx<T>)));
     CKM(ctx->E.ensure(chunk * N * sizeof(T)));
     CKM(ctx->E64.ensure(chunk * N * sizeof(double)));
-    if (sizeof(T) == 4) CKM(ctx->H64.ensure(chunk * NN * sizeof(cplx<double>)));
+    if (sizeof(T) == 4) CKM(ctx->H64.ensure(chunk * NN * sizeof(float4)));
     CKM(ctx->U.ensure(chunk * NN * sizeof(cplx<T>)));
     if (sizeof(T) == 4) CKM(ctx->Ulo.ensure(chunk * NN * sizeof(cplx<float>)));   // refined vectors' low parts
     CKM(ctx->HA.ensure(chunk * 6 * NN * sizeof(cplx<T>)));
@@ -248,7 +248,7 @@ int run_chunk(mepi_ctx* ctx, const KRange& kr, const JobDev* jb, int n_cta, doub
     double* E64 = ctx->E64.as<double>();
     if (mixed) {
         // FP64 H(k), FP32 Jacobi on it, FP64 residual refinement of the eigenpairs
-        cplx<double>* H64 = ctx->H64.as<cplx<double>>();
+        float4* H64 = ctx->H64.as<float4>();
         if (sep)
             STAGE(ST_FTH, launch_sep_h64(ctx->sep, kr, H64, ctx->stream));
         else

@@ -69,7 +69,7 @@ struct alignas(4 * sizeof(T)) RotPar {
 // updates in place -- one pass and two barriers per round.
 template <typename T, int NP>
 __global__ void __launch_bounds__(256) jacobi_kernel(int N, int64_t nk, int kblock, const cplx<T>* __restrict__ W,
-                                                     int nbW, const cplx<double>* __restrict__ H64,
+                                                     int nbW, const float4* __restrict__ Hdf,
                                                      T* __restrict__ E, cplx<T>* __restrict__ U, int max_sweeps,
                                                      int* sweeps_max, int* flag_cap, double degen_gap,
                                                      int* redo_flag, float gap_theta) {
@@ -103,9 +103,9 @@ __global__ void __launch_bounds__(256) jacobi_kernel(int N, int64_t nk, int kblo
             if (i < N && j < N) {
                 const int a = i < j ? i : j, b = i < j ? j : i;
                 cplx<T> h;
-                if (H64) {
-                    const cplx<double> x = H64[(size_t)k * NN + a * N + b];
-                    h = mk((T)x.re, (T)x.im);
+                if (Hdf) {
+                    const float4 x = Hdf[(size_t)k * NN + a * N + b];
+                    h = mk((T)x.x, (T)x.y);
                 } else {
                     h = W[(size_t)k * nbW * NN + a * N + b];
                 }
@@ -363,7 +363,7 @@ constexpr int JW_SMEM_FLOATS = 4 * 32 * JW_LD + 16 * 4 + 3 * 32;   // per warp: 
 
 template <int NW, int MB>
 __global__ void __launch_bounds__(32 * NW, MB) jacobi_warp_kernel(int N, int64_t nk, int kblock,
-                                                              const cplx<double>* __restrict__ H64,
+                                                              const float4* __restrict__ Hdf,
                                                               float* __restrict__ E, cplx<float>* __restrict__ U,
                                                               int max_sweeps, int* sweeps_max, int* flag_cap,
                                                               double degen_gap, int* redo_flag) {
@@ -387,16 +387,16 @@ __global__ void __launch_bounds__(32 * NW, MB) jacobi_warp_kernel(int N, int64_t
         if (k >= nk) break;
         const bool warm = jb > 0;
         // FP32 copy of the FP64 H(k), Hermitised from its upper triangle
-        const cplx<double>* Hk = H64 + (size_t)k * NN;
+        const float4* Hk = Hdf + (size_t)k * NN;
         float part = 0.f;
         for (int a = 0; a < 32; ++a) {
             const int b = lane;
             if (b >= a) {
                 float re = 0.f, im = 0.f;
                 if (b < N && a < N) {
-                    const cplx<double> x = Hk[a * N + b];
-                    re = (float)x.re;
-                    im = b == a ? 0.f : (float)x.im;
+                    const float4 x = Hk[a * N + b];
+                    re = x.x;
+                    im = b == a ? 0.f : x.y;
                 }
                 Hr[a * JW_LD + b] = re;
                 Hi[a * JW_LD + b] = im;
@@ -589,7 +589,7 @@ __global__ void __launch_bounds__(32 * NW, MB) jacobi_warp_kernel(int N, int64_t
 }  // namespace
 
 template <typename T>
-cudaError_t launch_eig(int N, int64_t nk, const cplx<T>* W, int nbW, const cplx<double>* H64, T* E, cplx<T>* U,
+cudaError_t launch_eig(int N, int64_t nk, const cplx<T>* W, int nbW, const float4* Hdf, T* E, cplx<T>* U,
                        int max_sweeps, int* sweeps_max, int* flag_cap, double degen_gap, int* redo_flag,
                        cudaStream_t s, int threads_req, int kblock_req, float gap_theta, bool warp_form) {
     if (nk <= 0) return cudaSuccess;
@@ -607,19 +607,19 @@ cudaError_t launch_eig(int N, int64_t nk, const cplx<T>* W, int nbW, const cplx<
         if (e == cudaSuccess)
             e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
         if (e != cudaSuccess) return e;
-        kern<<<grid, threads, smem, s>>>(N, nk, kblock, W, nbW, H64, E, U, max_sweeps, sweeps_max, flag_cap, degen_gap,
+        kern<<<grid, threads, smem, s>>>(N, nk, kblock, W, nbW, Hdf, E, U, max_sweeps, sweeps_max, flag_cap, degen_gap,
                                          redo_flag, gap_theta);
         return cudaGetLastError();
     };
     if constexpr (sizeof(T) == 4) {
-        if (warp_form && H64 && N <= 32) {
+        if (warp_form && Hdf && N <= 32) {
             constexpr int NW = 4;
             const unsigned g = (unsigned)((nk + (int64_t)kblock * NW - 1) / ((int64_t)kblock * NW));
             const size_t smem = (size_t)NW * JW_SMEM_FLOATS * sizeof(float);
             auto wgo = [&](auto kern) {
                 cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
                 if (e != cudaSuccess) return e;
-                kern<<<g, 32 * NW, smem, s>>>(N, nk, kblock, H64, reinterpret_cast<float*>(E),
+                kern<<<g, 32 * NW, smem, s>>>(N, nk, kblock, Hdf, reinterpret_cast<float*>(E),
                                               reinterpret_cast<cplx<float>*>(U), max_sweeps, sweeps_max, flag_cap,
                                               degen_gap, redo_flag);
                 return cudaGetLastError();
@@ -655,7 +655,7 @@ cudaError_t launch_eig(int N, int64_t nk, const cplx<T>* W, int nbW, const cplx<
 // unconverged FP32 Jacobi run (flag already set) or non-finite values is
 // flagged for the full FP64 rerun.  Eigenpairs are re-sorted by the refined
 // energies.
-__global__ void __launch_bounds__(256) refine_kernel(int N, const cplx<double>* __restrict__ H64,
+__global__ void __launch_bounds__(256) refine_kernel(int N, const float4* __restrict__ Hdf,
                                                      const float* __restrict__ lam, cplx<float>* __restrict__ U,
                                                      cplx<float>* __restrict__ Ulo, double* __restrict__ E64,
                                                      double degen_gap, int* __restrict__ redo_flag) {
@@ -678,17 +678,22 @@ __global__ void __launch_bounds__(256) refine_kernel(int N, const cplx<double>* 
     const int NN = N * N;
     for (int e = tid; e < NPP; e += nt) {
         const int i = e / Np, j = e % Np;
-        cplx<double> hv = mk(0.0, 0.0);
+        float4 x = make_float4(0.f, 0.f, 0.f, 0.f);
         cplx<float> uv = mk(0.f, 0.f);
         if (i < N && j < N) {
             const int a = i < j ? i : j, b = i < j ? j : i;
-            const cplx<double> x = H64[(size_t)k * NN + a * N + b];
-            hv = (i < j) ? x : (i > j) ? conjg(x) : mk(x.re, 0.0);
+            x = Hdf[(size_t)k * NN + a * N + b];
+            if (i > j) {          // lower triangle: the conjugate
+                x.y = -x.y;
+                x.w = -x.w;
+            } else if (i == j) {  // real diagonal
+                x.y = 0.f;
+                x.w = 0.f;
+            }
             uv = U[(size_t)k * NN + i * N + j];
         }
-        const cplx<float> hh = mk((float)hv.re, (float)hv.im);
-        Hh[e] = hh;
-        Hl[e] = mk((float)(hv.re - (double)hh.re), (float)(hv.im - (double)hh.im));
+        Hh[e] = mk(x.x, x.y);
+        Hl[e] = mk(x.z, x.w);
         Us[e] = uv;
     }
     for (int n = tid; n < Np; n += nt) ls[n] = n < N ? lam[(size_t)k * N + n] : 0.f;
@@ -813,14 +818,24 @@ __global__ void __launch_bounds__(256) refine_kernel(int N, const cplx<double>* 
             }
         } else {
             // the refined vector (u + U C) / |u + U C| as FP32 hi + lo: the sum by
-            // TwoSum, its norm in FP64, the scaling by TwoProduct (FMA)
-            double q = 0.0;
+            // TwoSum, its squared norm in double-FP32 (|h + e|^2 = h^2 + 2 h e + e^2,
+            // h^2 by TwoProduct, e^2 < 2^-48 h^2 dropped), the scaling by
+            // TwoProduct (FMA); FP64 only for the one square root per band
+            float qs = 0.f, qc = 0.f;
             for (int row = 0; row < N; ++row) {
                 const cplx<float> a = Us[row * Np + n], b = Ps[row * Np + n];
-                const double re = (double)a.re + (double)b.re, im = (double)a.im + (double)b.im;
-                q += re * re + im * im;
+                float hr, er, hm, em;
+                two_sum_f(a.re, b.re, hr, er);
+                two_sum_f(a.im, b.im, hm, em);
+                const float pr = hr * hr, pm = hm * hm;
+                float t, te;
+                two_sum_f(qs, pr, t, te);
+                float u, ue;
+                two_sum_f(t, pm, u, ue);
+                qs = u;
+                qc += te + ue + fmaf(hr, hr, -pr) + fmaf(hm, hm, -pm) + 2.f * (hr * er + hm * em);
             }
-            const double scd = 1.0 / sqrt(q);
+            const double scd = 1.0 / sqrt((double)qs + (double)qc);
             const float sch = (float)scd, scl = (float)(scd - (double)sch);
             for (int row = 0; row < N; ++row) {
                 const cplx<float> a = Us[row * Np + n], b = Ps[row * Np + n];
@@ -846,7 +861,7 @@ size_t refine_smem_bytes(int N) {
            5 * Np * Np * sizeof(cplx<float>);
 }
 
-cudaError_t launch_refine(int N, int64_t nk, const cplx<double>* H64, const float* lam, cplx<float>* U,
+cudaError_t launch_refine(int N, int64_t nk, const float4* Hdf, const float* lam, cplx<float>* U,
                           cplx<float>* Ulo, double* E64, double degen_gap, int* redo_flag, cudaStream_t s) {
     if (nk <= 0) return cudaSuccess;
     const size_t smem = refine_smem_bytes(N);
@@ -855,13 +870,13 @@ cudaError_t launch_refine(int N, int64_t nk, const cplx<double>* H64, const floa
         e = cudaFuncSetAttribute(refine_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
                                  cudaSharedmemCarveoutMaxShared);
     if (e != cudaSuccess) return e;
-    refine_kernel<<<(unsigned)nk, N <= 16 ? 128 : 256, smem, s>>>(N, H64, lam, U, Ulo, E64, degen_gap, redo_flag);
+    refine_kernel<<<(unsigned)nk, N <= 16 ? 128 : 256, smem, s>>>(N, Hdf, lam, U, Ulo, E64, degen_gap, redo_flag);
     return cudaGetLastError();
 }
 
-template cudaError_t launch_eig<double>(int, int64_t, const cplx<double>*, int, const cplx<double>*, double*,
+template cudaError_t launch_eig<double>(int, int64_t, const cplx<double>*, int, const float4*, double*,
                                         cplx<double>*, int, int*, int*, double, int*, cudaStream_t, int, int, float, bool);
-template cudaError_t launch_eig<float>(int, int64_t, const cplx<float>*, int, const cplx<double>*, float*,
+template cudaError_t launch_eig<float>(int, int64_t, const cplx<float>*, int, const float4*, float*,
                                        cplx<float>*, int, int*, int*, double, int*, cudaStream_t, int, int, float, bool);
 
 }  // namespace mepi

@@ -97,9 +97,10 @@ __global__ void __launch_bounds__(NT) ft_simt_kernel(DevModel m, KRange kr, cplx
 }
 // H(k) alone in FP64 for the mixed form's energy refinement: the same
 // contraction restricted to stack block 0 (read with the stack's block stride),
-// 8 k-points x 1 pair per thread, tau phase applied, H64[k][n][m] written.
+// 8 k-points x 1 pair per thread, tau phase applied, Hdf[k][n][m] written as
+// double-FP32 pairs (the FP64 value split once).
 constexpr int HK = 64, HP = 32;
-__global__ void __launch_bounds__(NT) ft_h64_kernel(DevModel m, KRange kr, cplx<double>* __restrict__ H64) {
+__global__ void __launch_bounds__(NT) ft_h64_kernel(DevModel m, KRange kr, float4* __restrict__ Hdf) {
     __shared__ cplx<double> Ps[RT][HK];
     __shared__ cplx<double> Ss[RT][HP];
     __shared__ double ks[HK][3];
@@ -166,17 +167,19 @@ __global__ void __launch_bounds__(NT) ft_h64_kernel(DevModel m, KRange kr, cplx<
             sincospi(2.0 * x, &sn, &cs);
             psi = mk(cs, sn);
         }
-        H64[(size_t)i * NN + pair] = psi * acc[j];
+        const cplx<double> x = psi * acc[j];
+        const float hr = (float)x.re, hi = (float)x.im;
+        Hdf[(size_t)i * NN + pair] = make_float4(hr, hi, (float)(x.re - (double)hr), (float)(x.im - (double)hi));
     }
 }
 
 }  // namespace
 
-cudaError_t launch_ft_h64(const DevModel& m, const KRange& kr, cplx<double>* H64, cudaStream_t s) {
+cudaError_t launch_ft_h64(const DevModel& m, const KRange& kr, float4* Hdf, cudaStream_t s) {
     if (kr.count <= 0) return cudaSuccess;
     const int NN = m.N * m.N;
     dim3 grid((unsigned)((kr.count + HK - 1) / HK), (unsigned)((NN + HP - 1) / HP));
-    ft_h64_kernel<<<grid, NT, 0, s>>>(m, kr, H64);
+    ft_h64_kernel<<<grid, NT, 0, s>>>(m, kr, Hdf);
     return cudaGetLastError();
 }
 

@@ -244,7 +244,7 @@ __global__ void __launch_bounds__(128) sep_w_kernel(DevModel m, KRange kr, const
     }
 }
 
-// H64[i][pair] = psi * sum_iz phase(kz) G2d[qx][qy][iz][0][pair] for KI items,
+// Hdf[i][pair] = psi * sum_iz phase(kz) G2d[qx][qy][iz][0][pair] for KI items,
 // the FP64 H(k) of the mixed form, in double-FP32: the FP64 slab values and
 // phases are split into FP32 hi + lo parts, each product a b of two such
 // pairs is formed as p + e (p = ah bh, e = fma(ah, bh, -p) + ah bl + al bh),
@@ -284,7 +284,7 @@ __device__ __forceinline__ void dfc_split(const DFc& v, cplx<float>& h, cplx<flo
 template <int KI>
 __global__ void __launch_bounds__(128) sep_h64_df_kernel(const cplx<double>* __restrict__ G2, KRange kr, int N,
                                                          int nbd, int nbz, int rz0, const double* __restrict__ tau,
-                                                         int qx0, int nqx, cplx<double>* __restrict__ H64) {
+                                                         int qx0, int nqx, float4* __restrict__ Hdf) {
     __shared__ ItemHead<double, KI> h;
     __shared__ cplx<float> phh[KI][32], phl[KI][32], fih[KI][kMaxN], fil[KI][kMaxN];
     const int NN = N * N;
@@ -348,7 +348,9 @@ __global__ void __launch_bounds__(128) sep_h64_df_kernel(const cplx<double>* __r
                 r = DFc{DF{0.f, 0.f}, DF{0.f, 0.f}};
                 dfc_mac(r, psh, psl, xh, xl);
             }
-            H64[(size_t)(i0 + it) * NN + pair] = mk((double)r.re.s + (double)r.re.c, (double)r.im.s + (double)r.im.c);
+            cplx<float> xh, xl;
+            dfc_split(r, xh, xl);
+            Hdf[(size_t)(i0 + it) * NN + pair] = make_float4(xh.re, xh.im, xl.re, xl.im);
         }
     }
 }
@@ -499,11 +501,11 @@ cudaError_t launch_w(const DevModel& m, const KRange& kr, const cplx<TG>* G2, in
 }
 }  // namespace
 
-cudaError_t launch_sep_h64(const SepPlan& p, const KRange& kr, cplx<double>* H64, cudaStream_t s) {
+cudaError_t launch_sep_h64(const SepPlan& p, const KRange& kr, float4* Hdf, cudaStream_t s) {
     if (kr.count <= 0) return cudaSuccess;
     const int NU = p.N * (p.N + 1) / 2, PT = pair_tile(NU);
     sep_h64_df_kernel<kItemsH><<<(unsigned)((kr.count + kItemsH - 1) / kItemsH), PT, 0, s>>>(
-        p.G2d, kr, p.N, p.nbd, p.nb[2], p.lo[2], p.tau, p.built_qx0, p.nqx, H64);
+        p.G2d, kr, p.N, p.nbd, p.nb[2], p.lo[2], p.tau, p.built_qx0, p.nqx, Hdf);
     return cudaGetLastError();
 }
 

@@ -401,12 +401,15 @@ struct AccLayout {
 template <typename T>
 cudaError_t launch_ft_simt(const DevModel& m, const KRange& kr, cplx<T>* W, cudaStream_t s);
 template <typename T>
-cudaError_t launch_eig(int N, int64_t nk, const cplx<T>* W, int nbW, const cplx<double>* H64, T* E, cplx<T>* U,
+cudaError_t launch_eig(int N, int64_t nk, const cplx<T>* W, int nbW, const float4* Hdf, T* E, cplx<T>* U,
                        int max_sweeps, int* sweeps_max, int* flag_cap, double degen_gap, int* redo_flag,
                        cudaStream_t s, int threads = 0, int kblock = 0, float gap_theta = 0.f,
                        bool warp_form = false);
-cudaError_t launch_ft_h64(const DevModel& m, const KRange& kr, cplx<double>* H64, cudaStream_t s);
-cudaError_t launch_refine(int N, int64_t nk, const cplx<double>* H64, const float* lam, cplx<float>* U, cplx<float>* Ulo, double* E64,
+// The mixed form's FP64-accurate H(k), upper triangle, as double-FP32 pairs: per
+// element float4 (re_hi, im_hi, re_lo, im_lo), hi = the value rounded to FP32,
+// lo = the rest rounded to FP32 (about 2^-48 relative).
+cudaError_t launch_ft_h64(const DevModel& m, const KRange& kr, float4* Hdf, cudaStream_t s);
+cudaError_t launch_refine(int N, int64_t nk, const float4* Hdf, const float* lam, cplx<float>* U, cplx<float>* Ulo, double* E64,
                           double degen_gap, int* redo_flag, cudaStream_t s);
 template <typename T>
 cudaError_t launch_rot(const DevModel& m, int64_t nk, const cplx<T>* W, const cplx<T>* U, cplx<T>* HA,
@@ -461,7 +464,7 @@ size_t sep_plan_want(const DevModel& m, const double* R_host, const int mp[3], b
 // enqueue the build of the slab that starts at qx0 (stream work only)
 cudaError_t launch_sep_slab(SepPlan& p, int qx0, cudaStream_t s);
 void sep_plan_free(SepPlan& p);
-cudaError_t launch_sep_h64(const SepPlan& p, const KRange& kr, cplx<double>* H64, cudaStream_t s);
+cudaError_t launch_sep_h64(const SepPlan& p, const KRange& kr, float4* Hdf, cudaStream_t s);
 template <typename T>
 cudaError_t launch_sep_w(const SepPlan& p, const DevModel& m, const KRange& kr, cplx<T>* W, cudaStream_t s);
 int bandsum_ctas();
