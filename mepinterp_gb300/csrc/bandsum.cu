@@ -850,10 +850,165 @@ cudaError_t launch_bandsum(const DevModel& m, const JobDev& j, int64_t nk, const
     return go(bandsum_kernel<T, false>);
 }
 
+// The FP32 form of opt_hall_kernel for N <= 32 and few (hbar omega, E_F) pairs:
+// one k-point per warp, lane n = band n, the sum over m in registers (no
+// shared-memory staging of V, no block barrier, no cross-lane reduction of the
+// per-band sums).  V is Hermitian (to the bit: the gauge step forms it so), so
+// lane n reads row n of V^i as the conjugate of column n, V^i(n, m) =
+// conj(V^i(m, n)), one coalesced row m per step, and with c^ij = V^i_nm V^j_mn
+// = v_i conj(v_j) the (m, n) products are conj(c^ij) and c^ji = conj(c^ij):
+//     vah^ij += 2 Im(c^ij) Wv            (vah^ji = -vah^ij, vah^ii = 0)
+//     koh^ij += c (g_mn) - c (g_nm) regrouped as (A + B, C - D), koh^ji = (A - B, C + D)
+// with A = Re c (g2r - g1r), B = Im c (g2i + g1i), C = Re c (g2i - g1i),
+// D = Im c (g2r + g1r): 24 double-FP32 sums per lane instead of 36.  The
+// occupation contraction sum_n f_n Y_n is a double-FP32 butterfly across the
+// lanes; each warp keeps its k-points' sums in shared memory and the CTA adds
+// its warps' sums to its slice in a fixed order.
+constexpr int OHW_WARPS = 8;
+constexpr int OHW_MAX_PAIRS = 32;   // (hbar omega, E_F) pairs per launch in this form
+
+__device__ __forceinline__ void ohw_df_warp_sum(float& s, float& c) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const float s2 = __shfl_xor_sync(0xffffffffu, s, o), c2 = __shfl_xor_sync(0xffffffffu, c, o);
+        const float t = s + s2, bb = t - s;
+        const float e = (s - (t - bb)) + (s2 - bb);
+        s = t;
+        c = c + c2 + e;
+    }
+}
+
+__global__ void __launch_bounds__(32 * OHW_WARPS, 2) opt_hall_warp_kernel(DevModel md, JobDev jb, int64_t nk,
+                                                                      const double* __restrict__ Eg,
+                                                                      const cplx<float>* __restrict__ Vg,
+                                                                      const int* __restrict__ skip,
+                                                                      double* __restrict__ partials) {
+    extern __shared__ double ohw_acc[];   // [warp][(e * nW + w) * 36 + q]
+    const int N = md.N, NN = N * N;
+    const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+    const unsigned FULL = 0xffffffffu;
+    const int npair = jb.nW * jb.nE;
+    double* Aw = ohw_acc + (size_t)wp * npair * 36;
+    for (int i = lane; i < npair * 36; i += 32) Aw[i] = 0.0;
+    __syncwarp();
+    const float eta = (float)jb.eta;
+    const bool act = lane < N;
+    for (int64_t k = (int64_t)blockIdx.x * OHW_WARPS + wp; k < nk; k += (int64_t)gridDim.x * OHW_WARPS) {
+        if (skip && skip[k]) continue;
+        const double En = act ? Eg[(size_t)k * N + lane] : 0.0;
+        const float eh = (float)En, el = (float)(En - (double)eh);
+        const cplx<float>* Vk = Vg + (size_t)k * 3 * NN;
+        for (int w = 0; w < jb.nW; ++w) {
+            const double hwd = jb.hw[w];
+            const float hwh = (float)hwd, hwl = (float)(hwd - (double)hwh);
+            DF acc[24];
+#pragma unroll
+            for (int q = 0; q < 24; ++q) acc[q] = DF{0.f, 0.f};
+            for (int m = 0; m < N; ++m) {
+                cplx<float> v[3];
+#pragma unroll
+                for (int i = 0; i < 3; ++i) v[i] = act ? conjg(Vk[(size_t)(i * N + m) * N + lane]) : mk(0.f, 0.f);
+                const float ehm = __shfl_sync(FULL, eh, m), elm = __shfl_sync(FULL, el, m);
+                if (!act || m == lane) continue;
+                float dh, dl;
+                df_diff(eh, el, ehm, elm, dh, dl);
+                const float d = dh + dl;
+                const float dm = ((dh - hwh) + dl) - hwl;
+                const float dp = ((dh + hwh) + dl) + hwl;
+                const float ar = dm * dp + eta * eta, ai = 2.f * hwh * eta;
+                const float an = 1.f / (ar * ar + ai * ai);
+                const float wvr = ar * an, wvi = ai * an;
+                const float b1r = d * dp, b1i = d * eta, b2r = d * dm, b2i = -d * eta;
+                const float n1 = 1.f / (b1r * b1r + b1i * b1i), n2 = 1.f / (b2r * b2r + b2i * b2i);
+                const float g1r = b1i * n1, g1i = b1r * n1, g2r = b2i * n2, g2i = b2r * n2;
+                const float gar = g2r - g1r, gbi = g2i + g1i, gci = g2i - g1i, gdr = g2r + g1r;
+#pragma unroll
+                for (int pq = 0; pq < 3; ++pq) {
+                    const int i = pq < 2 ? 0 : 1, j = pq == 0 ? 1 : 2;   // (x,y), (x,z), (y,z)
+                    const float cr = v[i].re * v[j].re + v[i].im * v[j].im;
+                    const float ci = v[i].im * v[j].re - v[i].re * v[j].im;
+                    const float dv = 2.f * ci;
+                    df_add(acc[6 * pq + 0], dv * wvr);
+                    df_add(acc[6 * pq + 1], dv * wvi);
+                    df_add(acc[6 * pq + 2], cr * gar);
+                    df_add(acc[6 * pq + 3], ci * gbi);
+                    df_add(acc[6 * pq + 4], cr * gci);
+                    df_add(acc[6 * pq + 5], ci * gdr);
+                }
+#pragma unroll
+                for (int i = 0; i < 3; ++i) {
+                    const float c = v[i].re * v[i].re + v[i].im * v[i].im;
+                    df_add(acc[18 + 2 * i], c * gar);
+                    df_add(acc[18 + 2 * i + 1], c * gci);
+                }
+            }
+            for (int e = 0; e < jb.nE; ++e) {
+                const float f = act ? (float)fd_stat<double>(En, jb.ef[e], jb.T_kelvin) : 0.f;
+                double* A = Aw + (size_t)(e * jb.nW + w) * 36;
+                // sum_n f_n Y_n[q] across the lanes, one value at a time
+                auto lane_sum = [&](const DF& y) -> double {
+                    const float p = f * y.s;
+                    float rs = p, rc = fmaf(f, y.c, fmaf(f, y.s, -p));
+                    ohw_df_warp_sum(rs, rc);
+                    return (double)rs + (double)rc;
+                };
+#pragma unroll
+                for (int pq = 0; pq < 3; ++pq) {
+                    const int i = pq < 2 ? 0 : 1, j = pq == 0 ? 1 : 2;
+                    const int qij = 2 * (i + 3 * j), qji = 2 * (j + 3 * i);
+                    const double vr = lane_sum(acc[6 * pq + 0]), vi = lane_sum(acc[6 * pq + 1]);
+                    const double ka = lane_sum(acc[6 * pq + 2]), kb = lane_sum(acc[6 * pq + 3]);
+                    const double kc = lane_sum(acc[6 * pq + 4]), kd = lane_sum(acc[6 * pq + 5]);
+                    if (lane == 0) {
+                        A[qij] += vr;
+                        A[qij + 1] += vi;
+                        A[qji] -= vr;
+                        A[qji + 1] -= vi;
+                        A[18 + qij] += ka + kb;
+                        A[18 + qij + 1] += kc - kd;
+                        A[18 + qji] += ka - kb;
+                        A[18 + qji + 1] += kc + kd;
+                    }
+                }
+#pragma unroll
+                for (int i = 0; i < 3; ++i) {
+                    const int qii = 2 * (i + 3 * i);
+                    const double ka = lane_sum(acc[18 + 2 * i]), kc = lane_sum(acc[18 + 2 * i + 1]);
+                    if (lane == 0) {
+                        A[18 + qii] += ka;
+                        A[18 + qii + 1] += kc;
+                    }
+                }
+                __syncwarp();
+            }
+        }
+    }
+    __syncthreads();
+    // the CTA's slice: its warps' sums added in warp order
+    const AccLayout L{jb.nE, jb.nval, jb.nW};
+    double* P = partials + (size_t)blockIdx.x * L.size();
+    for (int t = threadIdx.x; t < npair * 36; t += blockDim.x) {
+        double v = 0.0;
+        for (int u = 0; u < OHW_WARPS; ++u) v += ohw_acc[(size_t)u * npair * 36 + t];
+        const int ew = t / 36, q = t % 36;   // ew = e * nW + w
+        const int base = q < 18 ? L.vah_off() : L.koh_off();
+        P[base + (q % 18) + 18 * ew] += v;
+    }
+}
+
 template <typename T>
 cudaError_t launch_opt_hall(const DevModel& m, const JobDev& j, int64_t nk, const double* E, const cplx<T>* V,
                             const int* skip, double* partials, int n_cta, cudaStream_t s) {
     if (nk <= 0 || j.nW <= 0) return cudaSuccess;
+    if (sizeof(T) == 4 && m.N <= 32 && j.nW * j.nE <= OHW_MAX_PAIRS) {
+        const size_t smem = (size_t)OHW_WARPS * j.nW * j.nE * 36 * sizeof(double);
+        cudaError_t e = cudaFuncSetAttribute(opt_hall_warp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem);
+        if (e != cudaSuccess) return e;
+        opt_hall_warp_kernel<<<n_cta, 32 * OHW_WARPS, smem, s>>>(m, j, nk, E, reinterpret_cast<const cplx<float>*>(V),
+                                                                  skip, partials);
+        return cudaGetLastError();
+    }
     const size_t N = m.N, ET = sizeof(T) == 4 ? 64 : 8;
     size_t smem = 3 * N * (N + 1) * sizeof(cplx<T>) + (N * 36 + ET * N) * sizeof(T);
     if (sizeof(T) == 4) smem += (N * 36 + 2 * N * N + 8 * 32 * 36) * sizeof(T);   // Yc, dEh, dEl, part

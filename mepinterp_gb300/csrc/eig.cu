@@ -358,6 +358,29 @@ __device__ __forceinline__ float jw_pick(const float (&v)[32], int idx) {
     return (idx & 16) ? a[1] : a[0];
 }
 
+// (v[idx & ~1], v[idx | 1]) for a run-time idx: the select tree of jw_pick on
+// index bits 1..4, carried for both members of the pair
+__device__ __forceinline__ void jw_pick_pair(const float (&v)[32], int idx, float& e0, float& e1) {
+    float a[8], b[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        a[j] = (idx & 2) ? v[4 * j + 2] : v[4 * j];
+        b[j] = (idx & 2) ? v[4 * j + 3] : v[4 * j + 1];
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        a[j] = (idx & 4) ? a[2 * j + 1] : a[2 * j];
+        b[j] = (idx & 4) ? b[2 * j + 1] : b[2 * j];
+    }
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+        a[j] = (idx & 8) ? a[2 * j + 1] : a[2 * j];
+        b[j] = (idx & 8) ? b[2 * j + 1] : b[2 * j];
+    }
+    e0 = (idx & 16) ? a[1] : a[0];
+    e1 = (idx & 16) ? b[1] : b[0];
+}
+
 constexpr int JW_LD = 33;
 constexpr int JW_SMEM_FLOATS = 4 * 32 * JW_LD + 16 * 4 + 3 * 32;   // per warp: H, V planes, pair parameters, E/rank/player
 
@@ -478,8 +501,10 @@ __global__ void __launch_bounds__(32 * NW, MB) jacobi_warp_kernel(int N, int64_t
                 const int pl = jw_slot(pqp == 0 ? 0 : (pqp - 1 - r + 62) % 31 + 1);
                 const bool even = !(sl & 1);
                 // pair (p, q) = (even slot, odd slot): parameters formed by the even lane
-                const float d = jw_pick(mr, sl);
-                const float xr0 = jw_pick(mr, sl ^ 1), xi0 = jw_pick(mi, sl ^ 1);
+                float e0, e1;
+                jw_pick_pair(mr, sl, e0, e1);
+                const float d = even ? e0 : e1, xr0 = even ? e1 : e0;
+                const float xi0 = jw_pick(mi, sl ^ 1);
                 const float dq = __shfl_sync(FULL, d, pl);
                 float c = 1.f, sn = 0.f, pr = 1.f, pi = 0.f;
                 if (even && lane < N && pl < N) {
@@ -672,6 +697,9 @@ __global__ void __launch_bounds__(256) refine_kernel(int N, const float4* __rest
     cplx<float>* Rs = Us + NPP;
     cplx<float>* Ps = Rs + NPP;
     __shared__ float ls[kMaxN], rh[kMaxN], rl[kMaxN];
+    __shared__ float qp[2][8][kMaxN], sch_s[kMaxN], scl_s[kMaxN];
+    __shared__ long long ekey[kMaxN];
+    __shared__ int rk[kMaxN];
     __shared__ int s_flag;
     const int tid = threadIdx.x, nt = blockDim.x;
     const int64_t k = blockIdx.x;
@@ -751,7 +779,8 @@ __global__ void __launch_bounds__(256) refine_kernel(int N, const float4* __rest
     }
     __syncthreads();
     for (int n = tid; n < N; n += nt) {
-        const double r = (double)ls[n] + (double)Ps[n * Np + n].re / Sn[n];
+        // the Rayleigh-quotient correction P_nn / S_nn (~1e-7 of E) in FP32: ~1e-14 of E
+        const double r = (double)ls[n] + (double)(Ps[n * Np + n].re / Sn[n]);
         rho[n] = r;
         rh[n] = (float)r;
         rl[n] = (float)(r - (double)rh[n]);
@@ -805,50 +834,80 @@ __global__ void __launch_bounds__(256) refine_kernel(int N, const float4* __rest
     // U C into Ps
     smem_cgemm<float, false>(Np, Np, Us, Rs, Ps, tid, nt);
     __syncthreads();
-    for (int n = tid; n < N; n += nt) {
-        const double en = En[n];
-        int rank = 0;
-        for (int j = 0; j < N; ++j) rank += (En[j] < en || (En[j] == en && j < n)) ? 1 : 0;
-        E64[(size_t)k * N + rank] = en;
-        if (!Ulo) {
-            const float sc = (float)(1.0 / sqrt(Sn[n]));
-            for (int row = 0; row < N; ++row) {
-                const cplx<float> u = Us[row * Np + n] + Ps[row * Np + n];
-                U[(size_t)k * NN + row * N + rank] = mk(u.re * sc, u.im * sc);
-            }
-        } else {
-            // the refined vector (u + U C) / |u + U C| as FP32 hi + lo: the sum by
-            // TwoSum, its squared norm in double-FP32 (|h + e|^2 = h^2 + 2 h e + e^2,
-            // h^2 by TwoProduct, e^2 < 2^-48 h^2 dropped), the scaling by
-            // TwoProduct (FMA); FP64 only for the one square root per band
+    // the refined vectors' squared norms |u + U C|^2 in double-FP32, eight row
+    // groups per band (|h + e|^2 = h^2 + 2 h e + e^2 with h + e = u + (U C) by
+    // TwoSum, h^2 by TwoProduct, e^2 < 2^-48 h^2 dropped)
+    if (Ulo)
+        for (int e = tid; e < 8 * Np; e += nt) {
+            const int n = e % Np, g = e / Np;
             float qs = 0.f, qc = 0.f;
-            for (int row = 0; row < N; ++row) {
-                const cplx<float> a = Us[row * Np + n], b = Ps[row * Np + n];
-                float hr, er, hm, em;
-                two_sum_f(a.re, b.re, hr, er);
-                two_sum_f(a.im, b.im, hm, em);
-                const float pr = hr * hr, pm = hm * hm;
+            if (n < N)
+                for (int row = g; row < N; row += 8) {
+                    const cplx<float> a = Us[row * Np + n], b = Ps[row * Np + n];
+                    float hr, er, hm, em;
+                    two_sum_f(a.re, b.re, hr, er);
+                    two_sum_f(a.im, b.im, hm, em);
+                    const float pr = hr * hr, pm = hm * hm;
+                    float t, te, u, ue;
+                    two_sum_f(qs, pr, t, te);
+                    two_sum_f(t, pm, u, ue);
+                    qs = u;
+                    qc += te + ue + fmaf(hr, hr, -pr) + fmaf(hm, hm, -pm) + 2.f * (hr * er + hm * em);
+                }
+            qp[0][g][n] = qs;
+            qp[1][g][n] = qc;
+        }
+    // energies ordered through their IEEE-754 bits as signed integers (the
+    // order of doubles, on the integer pipe)
+    for (int n = tid; n < N; n += nt) {
+        const long long b = __double_as_longlong(En[n]);
+        ekey[n] = b ^ ((b >> 63) & 0x7fffffffffffffffLL);
+    }
+    __syncthreads();
+    // per band: its rank, its energy, the scale 1 / |u + U C| (FP64 only for the
+    // one square root per band) as FP32 hi + lo
+    for (int n = tid; n < N; n += nt) {
+        const long long kn = ekey[n];
+        int rank = 0;
+        for (int j = 0; j < N; ++j) rank += (ekey[j] < kn || (ekey[j] == kn && j < n)) ? 1 : 0;
+        E64[(size_t)k * N + rank] = En[n];
+        rk[n] = rank;
+        if (Ulo) {
+            float qs = qp[0][0][n], qc = qp[1][0][n];
+            for (int g = 1; g < 8; ++g) {
                 float t, te;
-                two_sum_f(qs, pr, t, te);
-                float u, ue;
-                two_sum_f(t, pm, u, ue);
-                qs = u;
-                qc += te + ue + fmaf(hr, hr, -pr) + fmaf(hm, hm, -pm) + 2.f * (hr * er + hm * em);
+                two_sum_f(qs, qp[0][g][n], t, te);
+                qs = t;
+                qc += te + qp[1][g][n];
             }
             const double scd = 1.0 / sqrt((double)qs + (double)qc);
-            const float sch = (float)scd, scl = (float)(scd - (double)sch);
-            for (int row = 0; row < N; ++row) {
-                const cplx<float> a = Us[row * Np + n], b = Ps[row * Np + n];
-                float hr, er, hm, em;
-                two_sum_f(a.re, b.re, hr, er);
-                two_sum_f(a.im, b.im, hm, em);
-                const float pr = hr * sch, pm = hm * sch;
-                const float lr = fmaf(hr, sch, -pr) + (er * sch + hr * scl);
-                const float lm = fmaf(hm, sch, -pm) + (em * sch + hm * scl);
-                const float ur = pr + lr, um = pm + lm;   // renormalised pair
-                U[(size_t)k * NN + row * N + rank] = mk(ur, um);
-                Ulo[(size_t)k * NN + row * N + rank] = mk((pr - ur) + lr, (pm - um) + lm);
-            }
+            sch_s[n] = (float)scd;
+            scl_s[n] = (float)(scd - (double)sch_s[n]);
+        } else {
+            sch_s[n] = (float)(1.0 / sqrt(Sn[n]));
+        }
+    }
+    __syncthreads();
+    // the refined vectors, one element per thread: (u + U C) scaled, as FP32 hi + lo
+    // (TwoSum for the sum, TwoProduct (FMA) for the scaling) or FP32 alone
+    for (int e = tid; e < N * N; e += nt) {
+        const int row = e / N, n = e - row * N;
+        const cplx<float> a = Us[row * Np + n], b = Ps[row * Np + n];
+        const size_t o = (size_t)k * NN + row * N + rk[n];
+        const float sch = sch_s[n];
+        if (!Ulo) {
+            U[o] = mk((a.re + b.re) * sch, (a.im + b.im) * sch);
+        } else {
+            const float scl = scl_s[n];
+            float hr, er, hm, em;
+            two_sum_f(a.re, b.re, hr, er);
+            two_sum_f(a.im, b.im, hm, em);
+            const float pr = hr * sch, pm = hm * sch;
+            const float lr = fmaf(hr, sch, -pr) + (er * sch + hr * scl);
+            const float lm = fmaf(hm, sch, -pm) + (em * sch + hm * scl);
+            const float ur = pr + lr, um = pm + lm;   // renormalised pair
+            U[o] = mk(ur, um);
+            Ulo[o] = mk((pr - ur) + lr, (pm - um) + lm);
         }
     }
     __syncthreads();
