@@ -11,11 +11,13 @@
 // each digit an integer that FP16 holds exactly.  A digit product d_p e_q is
 // an integer of magnitude at most 2^16 and a K = 64 sum of them at most 2^22,
 // so the FP32 tensor-memory accumulator sums the (at most four) (p,q) pairs of
-// one level L = p + q exactly (|sum| <= 2^24).  Levels 2..5 are kept (10 digit
-// GEMMs): the product carries about 2^-33 relative error against the row
-// scales, below the FP32 rounding of the inputs, which matches the compensated
-// (Dot2) CUDA-core rotation it replaces for the velocity blocks and is more
-// accurate than the plain FP32 one for the connection and curvature blocks.
+// one level L = p + q exactly (|sum| <= 2^24).  For the tile of the velocity
+// blocks levels 2..5 are kept (10 digit GEMMs): the product carries about 2^-33
+// relative error against the row scales, below the FP32 rounding of the
+// inputs, which matches the compensated (Dot2) CUDA-core rotation it replaces.
+// The connection and curvature tiles use three digits and levels 2..4 (6 digit
+// GEMMs, about 2^-24 of the row scales), the accuracy of the plain FP32
+// rotation those blocks had on the CUDA cores.
 // The levels are combined in double-FP32 (TwoSum).  The refined eigenvectors
 // enter as FP32 hi + lo pairs, so U carries about 35 bits into the products.
 //
@@ -103,16 +105,17 @@ __device__ __forceinline__ void digits4(float hi, float lo, float (&d)[4]) {
     d[3] = rintf(r);
 }
 
-// write 8 consecutive K elements (one 16-byte chunk) of all four digits of
-// already scaled hi + lo values
+// write 8 consecutive K elements (one 16-byte chunk) of the first nd digits
+// of already scaled hi + lo values
 __device__ __forceinline__ void store_chunk(unsigned char* tile0, uint32_t dig_bytes, int row, int chunk,
-                                            const float (&vh)[8], const float (&vl)[8]) {
+                                            const float (&vh)[8], const float (&vl)[8], int nd = 4) {
     float d[8][4];
 #pragma unroll
     for (int i = 0; i < 8; ++i) digits4(vh[i], vl[i], d[i]);
     const uint32_t off = (uint32_t)((row >> 3) * 1024 + (row & 7) * 128 + (((chunk ^ row) & 7) << 4));
 #pragma unroll
     for (int p = 0; p < 4; ++p) {
+        if (p >= nd) break;
         __half2 h0 = __floats2half2_rn(d[0][p], d[1][p]), h1 = __floats2half2_rn(d[2][p], d[3][p]);
         __half2 h2 = __floats2half2_rn(d[4][p], d[5][p]), h3 = __floats2half2_rn(d[6][p], d[7][p]);
         uint4 u;
@@ -172,28 +175,36 @@ __device__ __forceinline__ void transpose32(float (&v)[32], int lane) {
     }
 }
 
-// 8 columns of the four level accumulators -> hi + lo per column
-__device__ __forceinline__ void load_levels8(uint32_t taddr, float (&hi)[8], float (&lo)[8]) {
+// 8 columns of the level accumulators (levels 2..nd+1) -> hi + lo per column
+__device__ __forceinline__ void load_levels8(uint32_t taddr, float (&hi)[8], float (&lo)[8], int nd = 4) {
     float p2[8], p3[8], p4[8], p5[8];
     tmem_ld8(taddr, p2);
     tmem_ld8(taddr + 64, p3);
     tmem_ld8(taddr + 128, p4);
-    tmem_ld8(taddr + 192, p5);
+    if (nd == 4) {
+        tmem_ld8(taddr + 192, p5);
+    } else {
+#pragma unroll
+        for (int i = 0; i < 8; ++i) p5[i] = 0.f;
+    }
     tmem_wait_ld();
 #pragma unroll
     for (int i = 0; i < 8; ++i) combine(p2[i], p3[i], p4[i], p5[i], hi[i], lo[i]);
 }
 
-// the ten digit GEMMs of one tile: levels L = p + q = 2..5 into columns 64 (L-2)
-__device__ __forceinline__ void issue_tile(uint32_t tmem, const unsigned char* A, const unsigned char* B, uint64_t* bar) {
+// the digit GEMMs of one tile: levels L = p + q = 2..nd+1 (p, q <= nd) into
+// columns 64 (L-2): ten GEMMs with four digits, six with three
+__device__ __forceinline__ void issue_tile(uint32_t tmem, const unsigned char* A, const unsigned char* B, uint64_t* bar,
+                                           int nd) {
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 #pragma unroll
     for (int L = 2; L <= 5; ++L) {
+        if (L > nd + 1) break;
         bool first = true;
 #pragma unroll
         for (int p = 1; p <= 4; ++p) {
             const int q = L - p;
-            if (q < 1 || q > 4) continue;
+            if (p > nd || q < 1 || q > nd) continue;
             const uint64_t ad = sw128_desc(A + (p - 1) * RT_A_DIG), bd = sw128_desc(B + (q - 1) * RT_B_DIG);
 #pragma unroll
             for (int kk = 0; kk < 4; ++kk) {
@@ -241,6 +252,11 @@ __global__ void __launch_bounds__(RT_THREADS, 2)
     const uint32_t tlane = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(32 * h);   // my lanes, my column half
     uint32_t phase = 0;
     int issued = 0;
+    // digits per operand in the current tile: four for the tile of the velocity
+    // blocks (H_x, H_y, H_z, A_x: about 2^-33 of the row scales), three for the
+    // connection and curvature tiles (about 2^-24, the FP32 level these blocks
+    // need: six digit GEMMs instead of ten, three levels to read back)
+    int nd = 4;
 
     // digit stores -> async proxy, then one thread issues the tile's MMAs
     auto launch_mma = [&]() {
@@ -248,7 +264,7 @@ __global__ void __launch_bounds__(RT_THREADS, 2)
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
         __syncthreads();
         if (tid == 0) {
-            issue_tile(tmem, Adig, Bdig, &S.bar);
+            issue_tile(tmem, Adig, Bdig, &S.bar, nd);
             ++issued;
         }
     };
@@ -312,6 +328,7 @@ __global__ void __launch_bounds__(RT_THREADS, 2)
         }
 
         for (int tile = 0; tile < ntile; ++tile) {
+            nd = tile == 0 ? 4 : 3;
             // ---- GEMM1 operand A: rows (q, n) = [X_r(n,:) | X_i(n,:)] of W block 1 + 4 tile + q ----
             const int blk = 4 * tile + q;            // 0-based rotated block (W block blk + 1)
             const bool present = blk < nblk;
@@ -360,7 +377,7 @@ __global__ void __launch_bounds__(RT_THREADS, 2)
                         vh[t] = xv[8 * c + t] * sc;
                         vl[t] = 0.f;
                     }
-                    store_chunk(Adig, RT_A_DIG, row, 4 * h + c, vh, vl);
+                    store_chunk(Adig, RT_A_DIG, row, 4 * h + c, vh, vl, nd);
                 }
             }
             launch_mma();
@@ -373,7 +390,7 @@ __global__ void __launch_bounds__(RT_THREADS, 2)
 #pragma unroll
             for (int c = 0; c < 4; ++c) {
                 float hi[8], lo[8];
-                load_levels8(tlane + 8 * c, hi, lo);
+                load_levels8(tlane + 8 * c, hi, lo, nd);
 #pragma unroll
                 for (int i = 0; i < 8; ++i) {
                     const int j = 8 * c + i;
@@ -417,7 +434,7 @@ __global__ void __launch_bounds__(RT_THREADS, 2)
 #pragma unroll 1
                 for (int c = 0; c < 4; ++c) {
                     float hi[8], lo[8];
-                    load_levels8(tlane + 8 * c, hi, lo);
+                    load_levels8(tlane + 8 * c, hi, lo, nd);
 #pragma unroll
                     for (int i = 0; i < 8; ++i) {
                         const int j = 8 * c + i;
@@ -427,7 +444,7 @@ __global__ void __launch_bounds__(RT_THREADS, 2)
                         const uint32_t off = sw_off(32 * q + j, kx);
 #pragma unroll
                         for (int p = 0; p < 4; ++p)
-                            *reinterpret_cast<__half*>(Adig + p * RT_A_DIG + off) = __float2half_rn(d[p]);
+                            if (p < nd) *reinterpret_cast<__half*>(Adig + p * RT_A_DIG + off) = __float2half_rn(d[p]);
                     }
                 }
             }
@@ -442,7 +459,7 @@ __global__ void __launch_bounds__(RT_THREADS, 2)
 #pragma unroll 1
                 for (int c = 0; c < 4; ++c) {
                     float hi[8], lo[8];
-                    load_levels8(tlane + 8 * c, hi, lo);
+                    load_levels8(tlane + 8 * c, hi, lo, nd);
 #pragma unroll
                     for (int i = 0; i < 8; ++i) {
                         const int j = 8 * c + i;
