@@ -317,6 +317,9 @@ __global__ void __launch_bounds__(256) bandsum_kernel(DevModel md, JobDev jb, in
     const T ttol = (T)md.kubo_tol;
 
     for (int64_t k = blockIdx.x; k < nk; k += gridDim.x) {
+        // the next k-point's velocities into L2 while this one is summed
+        if (tid < 3 && k + gridDim.x < nk)
+            l2_prefetch(Vg + ((size_t)(k + gridDim.x) * 3 + tid) * NN, (uint32_t)(NN * sizeof(cplx<T>)));
         if (skip && skip[k]) continue;
         __syncthreads();
         for (int e = tid; e < 3 * NN; e += nt) {

@@ -409,6 +409,9 @@ __global__ void __launch_bounds__(32 * NW, MB) jacobi_warp_kernel(int N, int64_t
         const int64_t k = chain * kblock + jb;
         if (k >= nk) break;
         const bool warm = jb > 0;
+        // the run's next H(k) into L2 while this one is diagonalised
+        if (lane == 0 && jb + 1 < kblock && k + 1 < nk)
+            l2_prefetch(Hdf + (size_t)(k + 1) * NN, (uint32_t)(NN * sizeof(float4)));
         // FP32 copy of the FP64 H(k), Hermitised from its upper triangle
         const float4* Hk = Hdf + (size_t)k * NN;
         float part = 0.f;
@@ -704,6 +707,16 @@ __global__ void __launch_bounds__(256) refine_kernel(int N, const float4* __rest
     const int tid = threadIdx.x, nt = blockDim.x;
     const int64_t k = blockIdx.x;
     const int NN = N * N;
+    {
+        // one CTA per k-point: H(k) and U of the k-point about two waves of
+        // resident CTAs ahead into L2
+        constexpr int64_t kAhead = 1024;
+        const int64_t ka = k + kAhead;
+        if (ka < (int64_t)gridDim.x) {
+            if (tid == 0) l2_prefetch(Hdf + (size_t)ka * NN, (uint32_t)(NN * sizeof(float4)));
+            if (tid == 32) l2_prefetch(U + (size_t)ka * NN, (uint32_t)(NN * sizeof(cplx<float>)));
+        }
+    }
     for (int e = tid; e < NPP; e += nt) {
         const int i = e / Np, j = e % Np;
         float4 x = make_float4(0.f, 0.f, 0.f, 0.f);

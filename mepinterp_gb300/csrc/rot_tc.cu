@@ -280,6 +280,18 @@ __global__ void __launch_bounds__(RT_THREADS, 2)
 
     bool ok = true;
     for (int64_t k = blockIdx.x; k < nk && ok; k += gridDim.x) {
+        // the next k-point of this CTA into L2 while this one is worked on: its W
+        // blocks (one prefetch per block) and eigenvectors
+        const int64_t kn = k + gridDim.x;
+        if (tid < nblk + 2 && kn < nk) {
+            const uint32_t bb = (uint32_t)(NN * sizeof(cplx<float>));
+            if (tid < nblk)
+                l2_prefetch(W + ((size_t)kn * nbW + 1 + tid) * NN, bb);
+            else if (tid == nblk)
+                l2_prefetch(Ug + (size_t)kn * NN, bb);
+            else if (Ulo)
+                l2_prefetch(Ulo + (size_t)kn * NN, bb);
+        }
         __syncthreads();
         // ---- U planes (hi parts, for the curvature diagonal and the B exponents) ----
         const cplx<float>* Uk = Ug + (size_t)k * NN;
