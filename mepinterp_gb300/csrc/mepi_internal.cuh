@@ -105,8 +105,6 @@ __device__ __forceinline__ void smem_cgemm(int N, int ld, const cplx<T>* __restr
     }
 }
 
-// Upper-triangle element u (row-major over n <= m) -> (n, m).  Row n holds
-// N - n elements and starts at off(n) = n (2N - n + 1) / 2.
 // Asynchronous prefetch of [p, p + bytes) into L2 (cp.async.bulk.prefetch.L2;
 // nothing to wait for).  Issued only for a 16-byte aligned start and a whole
 // number of 16-byte units inside the caller's buffer; otherwise a no-op.
@@ -115,6 +113,8 @@ __device__ __forceinline__ void l2_prefetch(const void* p, uint32_t bytes) {
     asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
 }
 
+// Upper-triangle element u (row-major over n <= m) -> (n, m).  Row n holds
+// N - n elements and starts at off(n) = n (2N - n + 1) / 2.
 __device__ __forceinline__ void upper_pair(int u, int N, int& n, int& mm) {
     const float b = 2.f * N + 1.f;
     int r = (int)((b - sqrtf(b * b - 8.f * u)) * 0.5f);
