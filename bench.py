@@ -42,15 +42,16 @@ METRIC = "k-points/s for AHE+MEP, nWf=32"
 # measured DRAM bytes per k-point by (workload, form, stage): ncu captures of
 # the tb32 model on a 32^3 mesh, one 32,768-k launch per kernel
 NCU_DRAM_BYTES_PER_K = {
-    ("tb32_r3_k128", "mixed", "rot"): (2.08e9 + 1.60e9) / 32768,
-    ("tb32_r3_k128", "mixed", "eig"): (0.339e9 + 0.230e9) / 32768,
-    ("tb32_r3_k128", "mixed", "refine"): (0.609e9 + 0.238e9) / 32768,
+    ("tb32_r3_k128", "mixed", "rot"): (2.35e9 + 1.60e9) / 32768,       # rot_tc_kernel
+    ("tb32_r3_k128", "mixed", "eig"): (0.5125e9 + 0.2367e9) / 32768,   # jacobi_warp_kernel<4, 1>
+    ("tb32_r3_k128", "mixed", "refine"): (0.8037e9 + 0.4934e9) / 32768,
+    ("tb32_r3_k128", "mixed", "bandsum"): (0.8193e9 + 0.0111e9) / 32768,
     ("tb32_r3_k128", "mixed", "gauge"): (1.64e9 + 0.779e9) / 32768,
     ("tb32_r3_k128", "mixed", "fth"): (0.0895e9 + 0.231e9) / 32768,
 }
 UNIT = "k-points/s"
 # stages whose dominant kernel issues tcgen05 MMAs, by the pipe they run on
-TC_STAGES = {}
+TC_STAGES = {"rot": "tcgen05 kind::f16 (exact-slice FP16 digit products), digit formation on the CUDA cores"}
 
 
 def parse():
@@ -363,12 +364,13 @@ def run_gpu(args, rank, world):
         # (a seconds-long cuBLAS loop under the power cap) is its denominator
         tensor = peaks.get("bf16_tflops_sustained", 1700.0)
         achieved = flops_per_launch / avg_launch_s / 1e12
-        pipe = TC_STAGES.get(dom) or ("fp32 FMA (CUDA cores)" if mixed and dom != "fth" else "fp64 FMA (CUDA cores)")
+        tc_pipe = TC_STAGES.get(dom) if mixed and model.n_wf <= 32 else None   # rot_tc_kernel: mixed form, N <= 32
+        pipe = tc_pipe or ("fp32 FMA (CUDA cores)" if mixed and dom != "fth" else "fp64 FMA (CUDA cores)")
         roofline = {"bound": "tensor", "kernel": dom, "pipe": pipe, "achieved": achieved, "peak": tensor,
                     "unit": "TFLOP/s", "frac": achieved / tensor,
                     "peak_source": ("of measured" if "bf16_tflops_sustained" in peaks else "of fallback")
                     + " sustained bf16 tensor peak"}
-        if not TC_STAGES.get(dom):
+        if not tc_pipe:
             # context only: the nominal rate of the pipe it does run on, at the
             # median SM clock sampled during the timed region
             mhz = (clk or {}).get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
