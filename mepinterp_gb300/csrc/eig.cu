@@ -688,7 +688,7 @@ __global__ void __launch_bounds__(256) refine_kernel(int N, const float4* __rest
                                                      cplx<float>* __restrict__ Ulo, double* __restrict__ E64,
                                                      double degen_gap, int* __restrict__ redo_flag) {
     extern __shared__ unsigned char smem_raw[];
-    const int Np = N + (N & 1), NPP = Np * Np, h = Np / 2;
+    const int Np = N + (N & 1), NPP = Np * Np;
     double* rho = reinterpret_cast<double*>(smem_raw);
     double* En = rho + Np;
     float* Sn = reinterpret_cast<float*>(En + Np);
@@ -740,47 +740,43 @@ __global__ void __launch_bounds__(256) refine_kernel(int N, const float4* __rest
     for (int n = tid; n < Np; n += nt) ls[n] = n < N ? lam[(size_t)k * N + n] : 0.f;
     if (tid == 0) s_flag = redo_flag ? redo_flag[k] : 0;
     __syncthreads();
-    // R = H U - U diag(lambda), 2 x 2 tiles per thread: H_hi U in Dot2, H_lo U in FP32
-    for (int t = tid; t < h * h; t += nt) {
-        const int i = 2 * (t / h), c = 2 * (t % h);
-        DF sr[2][2], si[2][2];
-        cplx<float> lo[2][2];
+    // R = H U - U diag(lambda), 4 x 1 tiles per thread (four rows of a warp, its
+    // lanes over the columns: broadcast H loads, conflict-free U loads): H_hi U
+    // in Dot2, H_lo U in FP32
+    for (int t = tid; t < ((Np + 3) >> 2) * Np; t += nt) {
+        const int rb = t / Np, c = t - rb * Np, i0 = 4 * rb;
+        DF sr[4], si[4];
+        cplx<float> lo[4];
 #pragma unroll
-        for (int x = 0; x < 2; ++x)
-#pragma unroll
-            for (int y = 0; y < 2; ++y) {
-                sr[x][y] = DF{0.f, 0.f};
-                si[x][y] = DF{0.f, 0.f};
-                lo[x][y] = mk(0.f, 0.f);
-            }
+        for (int x = 0; x < 4; ++x) {
+            sr[x] = DF{0.f, 0.f};
+            si[x] = DF{0.f, 0.f};
+            lo[x] = mk(0.f, 0.f);
+        }
         for (int l = 0; l < Np; ++l) {
-            const cplx<float> h0 = Hh[i * Np + l], h1 = Hh[(i + 1) * Np + l];
-            const cplx<float> g0 = Hl[i * Np + l], g1 = Hl[(i + 1) * Np + l];
-            const cplx<float> u0 = Us[l * Np + c], u1 = Us[l * Np + c + 1];
-            const cplx<float> hx[2] = {h0, h1}, gx[2] = {g0, g1}, uy[2] = {u0, u1};
+            const cplx<float> u = Us[l * Np + c];
 #pragma unroll
-            for (int x = 0; x < 2; ++x)
-#pragma unroll
-                for (int y = 0; y < 2; ++y) {
-                    df_add_prod(sr[x][y], hx[x].re, uy[y].re);
-                    df_add_prod(sr[x][y], -hx[x].im, uy[y].im);
-                    df_add_prod(si[x][y], hx[x].re, uy[y].im);
-                    df_add_prod(si[x][y], hx[x].im, uy[y].re);
-                    fma_c(lo[x][y], gx[x], uy[y]);
-                }
+            for (int x = 0; x < 4; ++x) {
+                if (i0 + x >= Np) break;
+                const cplx<float> hx = Hh[(i0 + x) * Np + l], gx = Hl[(i0 + x) * Np + l];
+                df_add_prod(sr[x], hx.re, u.re);
+                df_add_prod(sr[x], -hx.im, u.im);
+                df_add_prod(si[x], hx.re, u.im);
+                df_add_prod(si[x], hx.im, u.re);
+                fma_c(lo[x], gx, u);
+            }
         }
 #pragma unroll
-        for (int x = 0; x < 2; ++x)
-#pragma unroll
-            for (int y = 0; y < 2; ++y) {
-                const int r = i + x, col = c + y;
-                const cplx<float> u = Us[r * Np + col];
-                // subtract lambda u exactly, then round the residual once
-                DF qr = sr[x][y], qi = si[x][y];
-                df_add_prod(qr, -ls[col], u.re);
-                df_add_prod(qi, -ls[col], u.im);
-                Rs[r * Np + col] = mk(qr.s + (qr.c + lo[x][y].re), qi.s + (qi.c + lo[x][y].im));
-            }
+        for (int x = 0; x < 4; ++x) {
+            const int r = i0 + x;
+            if (r >= Np) break;
+            const cplx<float> u = Us[r * Np + c];
+            // subtract lambda u exactly, then round the residual once
+            DF qr = sr[x], qi = si[x];
+            df_add_prod(qr, -ls[c], u.re);
+            df_add_prod(qi, -ls[c], u.im);
+            Rs[r * Np + c] = mk(qr.s + (qr.c + lo[x].re), qi.s + (qi.c + lo[x].im));
+        }
     }
     __syncthreads();
     // P = U^dag R (FP32)

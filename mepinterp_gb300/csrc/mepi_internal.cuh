@@ -70,38 +70,32 @@ template <typename T> __host__ __device__ __forceinline__ cplx<T> times_i(cplx<T
 template <typename T> __host__ __device__ __forceinline__ T abs2(cplx<T> a) { return a.re * a.re + a.im * a.im; }
 
 // C = op(A) B for N x N complex matrices in shared memory (row stride ld),
-// op(A) = A (adjA = false) or A^dag (adjA = true).  Each thread computes 2x2
-// output tiles so every shared-memory load feeds two complex multiply-adds.
-// Row/column N (odd N) reads zero padding the caller provides; only i, j < N
-// are written.  The caller synchronises before and after.
+// op(A) = A (adjA = false) or A^dag (adjA = true).  Each thread computes a
+// 4 x 1 output tile (four rows, one column): with N = 32 a warp shares its four
+// rows, so its A loads are broadcasts, and walks 32 consecutive columns of B,
+// so no load of the warp meets a bank conflict; every B load feeds four
+// complex multiply-adds.  Only i, j < N are read and written.  The caller
+// synchronises before and after.
 template <typename T, bool adjA>
 __device__ __forceinline__ void smem_cgemm(int N, int ld, const cplx<T>* __restrict__ A, const cplx<T>* __restrict__ B,
                                            cplx<T>* __restrict__ Cm, int tid, int nt) {
-    const int h = (N + 1) >> 1;
-    for (int t = tid; t < h * h; t += nt) {
-        const int i0 = 2 * (t / h), j0 = 2 * (t % h);
-        cplx<T> c00 = mk((T)0, (T)0), c01 = c00, c10 = c00, c11 = c00;
+    const int nrb = (N + 3) >> 2;
+    for (int t = tid; t < nrb * N; t += nt) {
+        const int rb = t / N, j = t - rb * N, r0 = 4 * rb;
+        cplx<T> c[4];
+#pragma unroll
+        for (int x = 0; x < 4; ++x) c[x] = mk((T)0, (T)0);
         for (int l = 0; l < N; ++l) {
-            cplx<T> a0, a1;
-            if (adjA) {
-                a0 = conjg(A[l * ld + i0]);
-                a1 = conjg(A[l * ld + i0 + 1]);
-            } else {
-                a0 = A[i0 * ld + l];
-                a1 = A[(i0 + 1) * ld + l];
+            const cplx<T> b = B[l * ld + j];
+#pragma unroll
+            for (int x = 0; x < 4; ++x) {
+                const int r = r0 + x;
+                if (r < N) fma_c(c[x], adjA ? conjg(A[l * ld + r]) : A[r * ld + l], b);
             }
-            const cplx<T> b0 = B[l * ld + j0], b1 = B[l * ld + j0 + 1];
-            fma_c(c00, a0, b0);
-            fma_c(c01, a0, b1);
-            fma_c(c10, a1, b0);
-            fma_c(c11, a1, b1);
         }
-        Cm[i0 * ld + j0] = c00;
-        if (j0 + 1 < N) Cm[i0 * ld + j0 + 1] = c01;
-        if (i0 + 1 < N) {
-            Cm[(i0 + 1) * ld + j0] = c10;
-            if (j0 + 1 < N) Cm[(i0 + 1) * ld + j0 + 1] = c11;
-        }
+#pragma unroll
+        for (int x = 0; x < 4; ++x)
+            if (r0 + x < N) Cm[(r0 + x) * ld + j] = c[x];
     }
 }
 

@@ -11,8 +11,9 @@
 // One k-point per CTA: U and the operand (mirrored from its upper triangle,
 // every W-gauge block being Hermitian) are staged in shared memory (padded
 // to an even size with zeros) and each product is an N x N x N complex
-// contraction in which every thread computes 2 x 2 output tiles
-// (smem_cgemm), so each shared-memory load feeds two multiply-adds.
+// contraction in which every thread computes 4 x 1 output tiles
+// (smem_cgemm: broadcast loads of A, conflict-free loads of B, each feeding
+// four multiply-adds).
 // Without the gauge transformation the kernel copies the W-gauge blocks.
 #include "mepi_internal.cuh"
 
