@@ -137,7 +137,7 @@ __device__ __noinline__ void bandsum_pairs_gemm(const DevModel& md, const JobDev
             const int n0 = t / N, n = t - n0 * N;
             short id = -1;
             if (n != n0) {
-                const float d0n = Dt[n0 * N + n], a2 = d0n * d0n;
+                const float d0n = Dt[n0 * ld + n], a2 = d0n * d0n;
                 if (!(fabsf(a2 * dmin[n0]) > ttol)) {
                     const int e = atomicAdd(&s_cnt, 1);
                     if (e < kMaskCap) {
@@ -155,10 +155,10 @@ __device__ __noinline__ void bandsum_pairs_gemm(const DevModel& md, const JobDev
     const int cnt = mep ? min(s_cnt, kMaskCap) : 0;
     for (int e = warp; e < cnt; e += nwarps) {
         const int n0 = s_list[e] >> 8, n = s_list[e] & 255;
-        const float d0n = Dt[n0 * N + n], a2 = d0n * d0n;
+        const float d0n = Dt[n0 * ld + n], a2 = d0n * d0n;
         cplx<float> x[3] = {mk(0.f, 0.f), mk(0.f, 0.f), mk(0.f, 0.f)};
         const int m = lane;
-        if (m < N && m != n0 && fabsf(a2 * Dt[n0 * N + m]) > ttol) {
+        if (m < N && m != n0 && fabsf(a2 * Dt[n0 * ld + m]) > ttol) {
             cplx<float> vnm[3], wmo[3];
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
@@ -192,15 +192,15 @@ __device__ __noinline__ void bandsum_pairs_gemm(const DevModel& md, const JobDev
         for (int c = 0; c < 3; ++c) vnn[c] = V(c, n0, n0);
         for (int n = part; n < N; n += 8) {
             if (n == n0) continue;
-            const float d0n = Dt[n0 * N + n];   // E0 - En
-            const float i0n = Iv[n0 * N + n];   // 1 / (E0 - En)
+            const float d0n = Dt[n0 * ld + n];   // E0 - En
+            const float i0n = Iv[n0 * ld + n];   // 1 / (E0 - En)
             cplx<float> vi[3], vk[3];
 #pragma unroll
             for (int c = 0; c < 3; ++c) { vi[c] = V(c, n0, n); vk[c] = V(c, n, n0); }
             if (jb.do_ahc) {
                 // the pair term formed once from (a, b) = (min, max): + to band a, - to band b
                 const int a = n0 < n ? n0 : n, b = n0 < n ? n : n0;
-                const float iab = Iv[a * N + b];
+                const float iab = Iv[a * ld + b];
                 const float w = (n0 < n ? -2.f : 2.f) * iab * iab;
                 cplx<float> va[3], vb[3];
 #pragma unroll
@@ -244,7 +244,7 @@ __device__ __noinline__ void bandsum_pairs_gemm(const DevModel& md, const JobDev
                     } else {   // beyond the list's capacity: the guarded sum here
                         const float a2 = d0n * d0n;
                         for (int m = 0; m < N; ++m) {
-                            if (m == n0 || !(fabsf(a2 * Dt[n0 * N + m]) > ttol)) continue;
+                            if (m == n0 || !(fabsf(a2 * Dt[n0 * ld + m]) > ttol)) continue;
                             cplx<float> vnm[3], wmo[3], x[3];
 #pragma unroll
                             for (int c = 0; c < 3; ++c) {
@@ -284,7 +284,7 @@ __device__ __noinline__ void bandsum_pairs_gemm(const DevModel& md, const JobDev
 }
 
 template <typename T, bool kGemm>
-__global__ void __launch_bounds__(256) bandsum_kernel(DevModel md, JobDev jb, int64_t nk, const double* __restrict__ Eg,
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) bandsum_kernel(DevModel md, JobDev jb, int64_t nk, const double* __restrict__ Eg,
                                                       const cplx<T>* __restrict__ Vg, const T* __restrict__ CSVg,
                                                       const int* __restrict__ skip, double* __restrict__ partials,
                                                       int use_tab) {
@@ -301,10 +301,11 @@ __global__ void __launch_bounds__(256) bandsum_kernel(DevModel md, JobDev jb, in
     T* icv = lcn + 9 * N;                                         // [9][kMaxN] Niu IC
     T* lcv = icv + 9 * kMaxN;                                     // [9][kMaxN] Niu LC
     T* Cs = lcv + 9 * kMaxN;                                      // [kMaxN]
-    T* Dt = Cs + kMaxN;                                           // [N][N] E_a - E_b (difference formed in FP64)
-    T* Iv = Dt + NN;                                              // [N][N] 1 / (E_a - E_b), 0 on the diagonal
+    T* Dt = Cs + kMaxN;                                           // [N][ld] E_a - E_b (difference formed in FP64;
+                                                                  // rows padded: band-parallel walks conflict-free)
+    T* Iv = Dt + N * ld;                                          // [N][ld] 1 / (E_a - E_b), 0 on the diagonal
     // kGemm: W and G as [3][32][33] complex, and the nearest-band distance per band
-    cplx<T>* Ws = reinterpret_cast<cplx<T>*>((reinterpret_cast<uintptr_t>(Iv + NN) + 15) & ~uintptr_t(15));
+    cplx<T>* Ws = reinterpret_cast<cplx<T>*>((reinterpret_cast<uintptr_t>(Iv + N * ld) + 15) & ~uintptr_t(15));
     cplx<T>* Gs = Ws + 3 * 32 * 33;
     cplx<T>* GVl = Gs + 3 * 32 * 33;                              // [kMaskCap][3] masked Niu IC sums
     T* dmin = reinterpret_cast<T*>(GVl + 3 * kMaskCap);
@@ -344,15 +345,15 @@ __global__ void __launch_bounds__(256) bandsum_kernel(DevModel md, JobDev jb, in
                     const int a = e / N, b = e % N;
                     float d, dl;
                     df_diff(s_Eh[a], s_El[a], s_Eh[b], s_El[b], d, dl);
-                    Dt[e] = d;
-                    Iv[e] = (a == b) ? 0.f : 1.f / d;
+                    Dt[a * ld + b] = d;
+                    Iv[a * ld + b] = (a == b) ? 0.f : 1.f / d;
                 }
             } else {
                 for (int e = tid; e < NN; e += nt) {
                     const int a = e / N, b = e % N;
                     const T d = (T)(Es[a] - Es[b]);
-                    Dt[e] = d;
-                    Iv[e] = (a == b) ? (T)0 : (T)1 / d;
+                    Dt[a * ld + b] = d;
+                    Iv[a * ld + b] = (a == b) ? (T)0 : (T)1 / d;
                 }
             }
         }
@@ -363,18 +364,23 @@ __global__ void __launch_bounds__(256) bandsum_kernel(DevModel md, JobDev jb, in
                 for (int e = tid; e < 3 * 32 * 32; e += nt) {
                     const int l = e >> 10, m = (e >> 5) & 31, n0 = e & 31;
                     cplx<T> w = mk((T)0, (T)0);
-                    if (m < N && n0 < N && m != n0) w = Iv[n0 * N + m] * V(l, m, n0);
+                    // 1 / (E_n0 - E_m) = -(1 / (E_m - E_n0)) to the bit (the differences are
+                    // antisymmetric and the reciprocal sign-symmetric): read along the row
+                    // m, so that the lanes (n0) meet no bank conflict
+                    if (m < N && n0 < N && m != n0) w = -Iv[m * ld + n0] * V(l, m, n0);
                     Ws[(l * 32 + m) * 33 + n0] = w;
                 }
                 for (int n0 = tid; n0 < N; n0 += nt) {
                     T dm = (T)1e30;
                     for (int m = 0; m < N; ++m)
-                        if (m != n0) dm = fmin(dm, (T)fabs(Dt[n0 * N + m]));
+                        if (m != n0) dm = fmin(dm, (T)fabs(Dt[n0 * ld + m]));
                     dmin[n0] = dm;
                 }
                 __syncthreads();
                 for (int t = tid; t < 256; t += nt) {
-                    const int nb = 2 * (t >> 4), ob = 2 * (t & 15);
+                    // 2 x 2 tiles: rows nb, nb + 1 and columns ob, ob + 16 (consecutive
+                    // lanes on consecutive columns: conflict-free Ws loads, Gs stores)
+                    const int nb = 2 * (t >> 4), ob = t & 15;
                     cplx<T> acc[2][2][3];
 #pragma unroll
                     for (int i = 0; i < 2; ++i)
@@ -389,7 +395,7 @@ __global__ void __launch_bounds__(256) bandsum_kernel(DevModel md, JobDev jb, in
 #pragma unroll
                             for (int i = 0; i < 2; ++i) a[i][c] = (nb + i < N) ? V(c, nb + i, m) : mk((T)0, (T)0);
 #pragma unroll
-                            for (int jj = 0; jj < 2; ++jj) b[jj][c] = Ws[(c * 32 + m) * 33 + ob + jj];
+                            for (int jj = 0; jj < 2; ++jj) b[jj][c] = Ws[(c * 32 + m) * 33 + ob + 16 * jj];
                         }
 #pragma unroll
                         for (int i = 0; i < 2; ++i)
@@ -409,16 +415,16 @@ __global__ void __launch_bounds__(256) bandsum_kernel(DevModel md, JobDev jb, in
 #pragma unroll
                         for (int jj = 0; jj < 2; ++jj)
 #pragma unroll
-                            for (int c = 0; c < 3; ++c) Gs[(c * 32 + nb + i) * 33 + ob + jj] = acc[i][jj][c];
+                            for (int c = 0; c < 3; ++c) Gs[(c * 32 + nb + i) * 33 + ob + 16 * jj] = acc[i][jj][c];
                 }
                 __syncthreads();
             }
         }
         // energy differences (formed in FP64) and their inverses: tabulated when
         // they fit in shared memory, else formed on the fly
-        auto dE = [&](int a, int b) -> T { return use_tab ? Dt[a * N + b] : (T)(Es[a] - Es[b]); };
+        auto dE = [&](int a, int b) -> T { return use_tab ? Dt[a * ld + b] : (T)(Es[a] - Es[b]); };
         auto iE = [&](int a, int b) -> T {
-            return use_tab ? Iv[a * N + b] : (a == b ? (T)0 : (T)1 / (T)(Es[a] - Es[b]));
+            return use_tab ? Iv[a * ld + b] : (a == b ? (T)0 : (T)1 / (T)(Es[a] - Es[b]));
         };
 
         if constexpr (kGemm && sizeof(T) == 4) {
@@ -824,7 +830,7 @@ template <typename T>
 size_t bandsum_smem(int N, bool tables) {
     size_t b = 3 * (size_t)N * (N + 1) * sizeof(cplx<T>);
     b += (9 * (size_t)N + kMaxN) * sizeof(double);
-    b += (18 * (size_t)N + 18 * kMaxN + kMaxN + (tables ? 2 * (size_t)N * N : 0)) * sizeof(T);
+    b += (18 * (size_t)N + 18 * kMaxN + kMaxN + (tables ? 2 * (size_t)N * (N + 1) : 0)) * sizeof(T);
     return (b + 15) & ~(size_t)15;
 }
 
