@@ -14,11 +14,13 @@
 // (qx, qy) column share one G2 slab, so with the k-points ordered column by
 // column the slab is read from HBM once and from L2 by the rest of the column.
 //
-// Precision: the plan is built in FP64.  The FP64 form keeps G2 in FP64 for all
-// blocks.  The mixed form keeps all blocks in FP32 (nbz-term sums of FP32
-// values, about 1e-7 relative) for its per-k work, plus FP64 slabs for the
-// FP64-accurate H(k) of the eigenpair refinement (summed in double-FP32) and
-// for its FP64 reruns (all blocks when they fit in memory, else H alone).
+// Precision: the FP64 form's plan is built in FP64 and keeps G2 in FP64 for all
+// blocks.  The mixed form's plan sums over Rx in FP64 and over Ry in
+// double-FP32 (about 2^-46 relative, off the 1/64-rate FP64 pipe).  The mixed
+// form keeps all blocks in FP32 (nbz-term sums of FP32 values, about 1e-7
+// relative) for its per-k work, plus FP64 slabs for the FP64-accurate H(k) of
+// the eigenpair refinement (summed in double-FP32) and for its FP64 reruns (all
+// blocks when they fit in memory, else H alone).
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -41,8 +43,10 @@ __device__ __forceinline__ cplx<double> phase(double k, int R) {
 
 // G1[qx][iy][iz][e] = sum_ix phase(kx, Rx0 + ix) box[ix][iy][iz][e],  e = blk * NN + pair,
 // for the qx of one slab [qx0, qx0 + gridDim.z)
+// With df_out (the mixed form's plans) G1 is written as double-FP32 pairs,
+// float4 (re_hi, im_hi, re_lo, im_lo) in the same 16 bytes, for sep_stage_b_df.
 __global__ void sep_stage_a(const cplx<double>* __restrict__ box, cplx<double>* __restrict__ G1, int EL, int nbx,
-                            int nby, int nbz, int rx0, int n1, int qx0) {
+                            int nby, int nbz, int rx0, int n1, int qx0, bool df_out) {
     const int yz = blockIdx.y, qx = blockIdx.z;   // qx relative to the slab's first qx0
     __shared__ cplx<double> ph[32];
     if (threadIdx.x < nbx) ph[threadIdx.x] = phase(mp_coord(qx0 + qx, n1), rx0 + (int)threadIdx.x);
@@ -50,7 +54,13 @@ __global__ void sep_stage_a(const cplx<double>* __restrict__ box, cplx<double>* 
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < EL; e += gridDim.x * blockDim.x) {
         cplx<double> acc = mk(0.0, 0.0);
         for (int ix = 0; ix < nbx; ++ix) fma_c(acc, ph[ix], box[((size_t)ix * nby * nbz + yz) * EL + e]);
-        G1[((size_t)qx * nby * nbz + yz) * EL + e] = acc;
+        const size_t o = ((size_t)qx * nby * nbz + yz) * EL + e;
+        if (df_out) {
+            const float hr = (float)acc.re, hi = (float)acc.im;
+            reinterpret_cast<float4*>(G1)[o] = make_float4(hr, hi, (float)(acc.re - (double)hr), (float)(acc.im - (double)hi));
+        } else {
+            G1[o] = acc;
+        }
     }
 }
 
@@ -463,15 +473,54 @@ int sep_plan_build(SepPlan& p, const DevModel& m, const double* R_host, const cp
     return 0;
 }
 
+// sep_stage_b for the mixed form's plans, in double-FP32: G1 arrives as hi/lo
+// FP32 pairs (sep_stage_a with df_out), the ky phases are split once per CTA,
+// and the nby-term sums run in TwoSum/TwoProduct FP32 arithmetic (about 2^-46
+// relative) instead of on the 1/64-rate FP64 pipe.  G2f gets the FP32 rounding
+// of the sum, G2d (the first nbd blocks) the pair widened to FP64.
+__global__ void sep_stage_b_df(const float4* __restrict__ G1, cplx<double>* __restrict__ G2d,
+                               cplx<float>* __restrict__ G2f, int NN, int nbk, int nbd, int nby, int nbz, int ry0,
+                               int n1, int n2) {
+    const int iz = blockIdx.y % nbz, qy = blockIdx.y / nbz, qx = blockIdx.z;
+    __shared__ cplx<float> phh[32], phl[32];
+    if (threadIdx.x < nby) {
+        const cplx<double> p = phase(mp_coord(qy, n2), ry0 + (int)threadIdx.x);
+        split_d(p.re, phh[threadIdx.x].re, phl[threadIdx.x].re);
+        split_d(p.im, phh[threadIdx.x].im, phl[threadIdx.x].im);
+    }
+    __syncthreads();
+    const int EL = nbk * NN;
+    const size_t cell = ((size_t)qx * n2 + qy) * nbz + iz;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < EL; e += gridDim.x * blockDim.x) {
+        DFc acc{DF{0.f, 0.f}, DF{0.f, 0.f}};
+        for (int iy = 0; iy < nby; ++iy) {
+            const float4 x = G1[(((size_t)qx * nby + iy) * nbz + iz) * EL + e];
+            dfc_mac(acc, phh[iy], phl[iy], mk(x.x, x.y), mk(x.z, x.w));
+        }
+        cplx<float> h, l;
+        dfc_split(acc, h, l);
+        if (e < nbd * NN) G2d[cell * nbd * NN + e] = mk((double)h.re + (double)l.re, (double)h.im + (double)l.im);
+        G2f[cell * EL + e] = h;
+    }
+}
+
 cudaError_t launch_sep_slab(SepPlan& p, int qx0, cudaStream_t s) {
     const int nq = std::min(p.nqx, p.mp[0] - qx0);
     if (nq <= 0) return cudaErrorInvalidValue;
     const int EL = p.nbk * p.N * p.N;
     dim3 ga((EL + 255) / 256, p.nb[1] * p.nb[2], nq);
-    sep_stage_a<<<ga, 256, 0, s>>>(p.box, p.G1, EL, p.nb[0], p.nb[1], p.nb[2], p.lo[0], p.mp[0], qx0);
+    // the mixed form's plans (FP32 slabs for the per-k work, FP64 slabs that feed
+    // the double-FP32 H(k) and the FP64 reruns) are summed in double-FP32; the
+    // FP64 form's plans in FP64
+    const bool df = !p.fp64 && p.G2f;
+    sep_stage_a<<<ga, 256, 0, s>>>(p.box, p.G1, EL, p.nb[0], p.nb[1], p.nb[2], p.lo[0], p.mp[0], qx0, df);
     dim3 gb((EL + 255) / 256, p.mp[1] * p.nb[2], nq);
-    sep_stage_b<<<gb, 256, 0, s>>>(p.G1, p.G2d, p.G2f, p.N * p.N, p.nbk, p.nbd, p.nb[1], p.nb[2], p.lo[1], p.mp[0],
-                                   p.mp[1]);
+    if (df)
+        sep_stage_b_df<<<gb, 256, 0, s>>>(reinterpret_cast<const float4*>(p.G1), p.G2d, p.G2f, p.N * p.N, p.nbk, p.nbd,
+                                          p.nb[1], p.nb[2], p.lo[1], p.mp[0], p.mp[1]);
+    else
+        sep_stage_b<<<gb, 256, 0, s>>>(p.G1, p.G2d, p.G2f, p.N * p.N, p.nbk, p.nbd, p.nb[1], p.nb[2], p.lo[1], p.mp[0],
+                                       p.mp[1]);
     p.built_qx0 = qx0;
     return cudaGetLastError();
 }
