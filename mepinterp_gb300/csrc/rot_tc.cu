@@ -12,12 +12,13 @@
 // an integer of magnitude at most 2^16 and a K = 64 sum of them at most 2^22,
 // so the FP32 tensor-memory accumulator sums the (at most four) (p,q) pairs of
 // one level L = p + q exactly (|sum| <= 2^24).  For the tile of the velocity
-// blocks levels 2..5 are kept (10 digit GEMMs): the product carries about 2^-33
-// relative error against the row scales, below the FP32 rounding of the
-// inputs, which matches the compensated (Dot2) CUDA-core rotation it replaces.
-// The connection and curvature tiles use three digits and levels 2..4 (6 digit
-// GEMMs, about 2^-24 of the row scales), the accuracy of the plain FP32
-// rotation those blocks had on the CUDA cores.
+// blocks levels 2..5 are kept (10 digit GEMMs): at K = 64 the product is
+// typically within 2^-32 of the product of its row and column scales (2^-28 in
+// the worst case of extreme digits with aligned signs), below the FP32
+// rounding of the inputs, which matches the compensated (Dot2) CUDA-core
+// rotation it replaces.  The connection and curvature tiles use three digits
+// and levels 2..4 (6 digit GEMMs; typically 2^-23, at worst 2^-19), the
+// accuracy of the plain FP32 rotation those blocks had on the CUDA cores.
 // The levels are combined in double-FP32 (TwoSum).  The refined eigenvectors
 // enter as FP32 hi + lo pairs, so U carries about 35 bits into the products.
 //
@@ -253,9 +254,9 @@ __global__ void __launch_bounds__(RT_THREADS, 2)
     uint32_t phase = 0;
     int issued = 0;
     // digits per operand in the current tile: four for the tile of the velocity
-    // blocks (H_x, H_y, H_z, A_x: about 2^-33 of the row scales), three for the
-    // connection and curvature tiles (about 2^-24, the FP32 level these blocks
-    // need: six digit GEMMs instead of ten, three levels to read back)
+    // blocks (H_x, H_y, H_z, A_x: typically 2^-32 of the scales), three for the
+    // connection and curvature tiles (typically 2^-23, the FP32 level these
+    // blocks need: six digit GEMMs instead of ten, three levels to read back)
     int nd = 4;
 
     // digit stores -> async proxy, then one thread issues the tile's MMAs
