@@ -58,20 +58,24 @@ def _omega_norm(perk: np.ndarray) -> np.ndarray:
 def cell_features(perk: np.ndarray, n: int) -> np.ndarray:
     """(n^3, 31) features per coarse cell: k (3), log10 gap in eV (1), and
     log10(|Omega| / median |Omega| + 1e-3) of the cell and its 26 periodic
-    neighbours (27)."""
+    neighbours (27).  Written column by column into one FP32 array (the
+    neighbour columns rolled from the FP32 copy of the cell column)."""
     k = np.arange(n ** 3)
-    q = np.stack([k % n, (k // n) % n, k // (n * n)], axis=1)
-    kf = (2.0 * (q + 1) - n - 1) / (2.0 * n)
-    gap = np.log10(np.maximum(np.abs(perk[:, 3]) * 27.211385, 1e-6))
+    out = np.empty((n ** 3, N_FEATURES), np.float32)
+    q = (k % n, (k // n) % n, k // (n * n))
+    for a in range(3):
+        out[:, a] = (2.0 * (q[a] + 1) - n - 1) / (2.0 * n)
+    out[:, 3] = np.log10(np.maximum(np.abs(perk[:, 3]) * 27.211385, 1e-6))
     om = _omega_norm(perk)
     med = float(np.median(om)) or 1.0
-    lo = np.log10(om / med + 1e-3).reshape(n, n, n)      # [qz, qy, qx]
-    nb = []
+    lo = np.log10(om / med + 1e-3).astype(np.float32).reshape(n, n, n)      # [qz, qy, qx]
+    c = 4
     for dz in (-1, 0, 1):
         for dy in (-1, 0, 1):
             for dx in (-1, 0, 1):
-                nb.append(np.roll(lo, (-dz, -dy, -dx), axis=(0, 1, 2)).ravel())
-    return np.concatenate([kf, gap[:, None], np.stack(nb, axis=1)], axis=1).astype(np.float32)
+                out[:, c] = np.roll(lo, (-dz, -dy, -dx), axis=(0, 1, 2)).ravel()
+                c += 1
+    return out
 
 
 def _job(job: dict, n: int) -> dict:
@@ -154,7 +158,9 @@ def adaptive(ctx: api.Context, job: dict, n: int = 48, s: int = 6, frac: float =
         scale = float(np.median(om)) or 1.0
         lab = np.log10(cell_labels(f_s["perk"], perk[sample], s) / scale + 1e-3).astype(np.float32)
         mu, sd = feats.mean(axis=0), feats.std(axis=0) + 1e-6
-        x = (feats - mu) / sd
+        x = feats
+        x -= mu                       # in place: the same FP32 operations as (feats - mu) / sd
+        x /= sd
         lm, ls = float(lab.mean()), float(lab.std() + 1e-6)
         with Net(N_FEATURES, depth, seed=seed) as net:
             hist = net.train(x[sample], (lab - lm) / ls, epochs=epochs, batch=batch, lr=lr, seed=seed)
